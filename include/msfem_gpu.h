@@ -1,0 +1,221 @@
+/*
+ * msfem_gpu.h -- C-ABI of libmsfem_gpu.so, the GB300 (sm_103a) engine for the
+ * per-coarse-cell multiscale basis problems of an MsFEM discretisation of
+ * -div(A(x) grad u) = f.
+ *
+ * For every coarse cell K (a quadrilateral / hexahedron given by its 2^d
+ * corners in deal.II vertex order) the engine
+ *   1. builds the local N^d fine Q1 mesh (uniform refinement of K),
+ *   2. assembles the fine Q1 form  int_K grad(psi_i) . A(x) grad(psi_j)  with a
+ *      2^d-point Gauss rule per fine cell, and the load  int_K f psi_i,
+ *   3. solves the 2^d Dirichlet problems whose boundary data are the coarse
+ *      Q1 nodal functions (value 1 at coarse vertex i, 0 at the others),
+ *   4. integrates the coarse element matrix  M_ij = phi_i^T A phi_j  and the
+ *      coarse load  F_i = phi_i^T b  from those multiscale basis functions.
+ *
+ * Reference interfaces replaced (konsim83/MPI-Parallel-Multiscale-Diffusion-FEM):
+ *   msfem_run_batch      <- DiffusionProblemBasis<dim>::run()
+ *                           include/base/diffusion_problem_basis.tpp:438-474
+ *                           (make_grid :90-99, setup_system :102-156,
+ *                            assemble_system :159-242, solve_iterative :293-317,
+ *                            assemble_global_element_matrix :245-285)
+ *                           called once per owned cell by
+ *                           include/base/diffusion_problem_ms.tpp:81-87
+ *   M output             <- get_global_element_matrix()  diffusion_problem_basis.tpp:320-325
+ *   F output             <- get_global_element_rhs()     diffusion_problem_basis.tpp:328-333
+ *   basis output         <- solution_vector[i], read by set_global_weights()
+ *                           diffusion_problem_basis.tpp:352-377
+ *   msfem_coef_desc      <- Coefficients::MatrixCoeff<dim>::value_list
+ *                           include/coefficients/matrix_coeff.tpp:66-91,
+ *                           Coefficients::RightHandSide<dim>::value_list
+ *                           include/coefficients/right_hand_side.tpp:27-40
+ *   Dirichlet data       <- Coefficients::BasisQ1<dim>  include/coefficients/basis_q1.tpp:26-158
+ *   cell status / error  <- SolverControl::NoConvergence thrown by SolverCG
+ *                           diffusion_problem_basis.tpp:297-306
+ *
+ * Conventions
+ *   - All floating point input and output is IEEE FP64.
+ *   - Coarse-cell corners: corners[cell][v][c], v in deal.II lexicographic
+ *     vertex order (v = vx + 2 vy + 4 vz), c the coordinate.
+ *   - Local fine nodes are numbered lexicographically, x fastest:
+ *     node = ix + n (iy + n iz), n = N + 1.  (deal.II's own numbering is the
+ *     cell-traversal order; callers that need it permute by support point.)
+ *   - M[cell][i][j] is row-major with row i = test function, column j = trial,
+ *     exactly as global_element_matrix(i_test, i_trial).
+ *   - No pointer is retained after a call returns.  No C++ exception crosses
+ *     this boundary; every entry point returns an msfem_status_code.
+ *   - A handle is bound to one device and must not be used by two host
+ *     threads at the same time.  One MPI rank = one handle = one GPU.
+ */
+#ifndef MSFEM_GPU_H_
+#define MSFEM_GPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MSFEM_ABI_VERSION 1
+
+/* Largest supported local refinement per coarse cell. */
+#define MSFEM_MAX_N_2D 32
+#define MSFEM_MAX_N_3D 24
+
+typedef enum msfem_status_code {
+  MSFEM_OK = 0,
+  MSFEM_ERR_INVALID_ARG = -1,   /* malformed descriptor / size out of range */
+  MSFEM_ERR_CUDA = -2,          /* CUDA runtime error, see msfem_last_error */
+  MSFEM_ERR_NO_DEVICE = -3,     /* no usable sm_103 device */
+  MSFEM_ERR_UNSUPPORTED = -4,   /* combination not implemented */
+  MSFEM_ERR_OUT_OF_MEMORY = -5,
+  MSFEM_ERR_NOT_CONVERGED = -6  /* at least one cell did not reach tol: see cell_status */
+} msfem_status_code;
+
+/* Per-cell status word (cell_status output). */
+typedef enum msfem_cell_status {
+  MSFEM_CELL_CONVERGED = 0,
+  MSFEM_CELL_MAXIT = 1,         /* maxit reached (reference: SolverControl::NoConvergence) */
+  MSFEM_CELL_NAN = 2,           /* non-finite value met (bad coefficient, breakdown) */
+  MSFEM_CELL_BAD_INPUT = 3      /* e.g. degenerate / inverted cell geometry */
+} msfem_cell_status;
+
+/* Coefficient A(x) kinds.  Scalar kinds mean A = a(x) I. */
+typedef enum msfem_coef_kind {
+  /* A = const symmetric tensor; params = (a11,a12,a22) in 2D,
+   * (a11,a12,a13,a22,a23,a33) in 3D. */
+  MSFEM_COEF_CONSTANT = 0,
+  /* The reference's own Coefficients::MatrixCoeff<dim> (matrix_coeff.tpp:17-91):
+   * c(x) = 1 - 0.9999 (0.5 sin(2 PI_D 57 x) + 0.5 sin(2 PI_D 57 y)),
+   * A = R diag(c) R^T, PI_D = 3.14592653509793218403 as in coefficients.h:21,
+   * R the rotation by PI_D/3 (2D) or the ZXZ Euler matrix (PI_D/3, PI_D/6, PI_D/4) (3D). */
+  MSFEM_COEF_REFERENCE = 1,
+  /* a = 1 + amp sin(2 pi x/eps) sin(2 pi y/eps) [sin(2 pi z/eps) in 3D];
+   * params = (amp, eps). */
+  MSFEM_COEF_SINSIN = 2,
+  /* Random Fourier fields g_f(x) = sum_m amp_m cos(k_m . x + phase_m), table
+   * modes[f][m][5] = (kx, ky, kz, amp, phase).  2D: 3 fields (g1, g2, theta),
+   * A = R(theta) diag(exp g1, exp g2) R(theta)^T.  3D: 1 field, a = exp g1. */
+  MSFEM_COEF_FOURIER = 3,
+  /* a = 1 + (params[0] - 1) * [x inside any sphere]; spheres[s] = (cx,cy,cz,r)
+   * (2D: discs, cz ignored). */
+  MSFEM_COEF_SPHERES = 4,
+  /* Values at the Gauss points, caller-tabulated (generic path for any
+   * TensorFunction: tabulate with value_list and pass the values).  Per cell a
+   * block of ncomp * 2^d * N^d doubles, ordered [comp][q][fine cell], fine
+   * cells lexicographic (x fastest), q the deal.II QGauss(2) point order
+   * (x fastest).  ncomp = 1 (scalar) or d(d+1)/2 (symmetric tensor, component
+   * order as for CONSTANT). */
+  MSFEM_COEF_TABULATED = 5
+} msfem_coef_kind;
+
+typedef enum msfem_precision {
+  MSFEM_PREC_FP64 = 0,          /* plain FP64 Jacobi-PCG (the drop-in form) */
+  MSFEM_PREC_MIXED = 1          /* FP32 inner PCG + FP64 residual refinement */
+} msfem_precision;
+
+typedef enum msfem_memory {
+  MSFEM_MEM_HOST = 0,           /* all descriptor/output pointers are host memory */
+  MSFEM_MEM_DEVICE = 1          /* all descriptor/output pointers are device memory */
+} msfem_memory;
+
+typedef enum msfem_warm_start {
+  MSFEM_WARM_NONE = 0,          /* x0 = 0 in the interior (reference behaviour) */
+  MSFEM_WARM_USER = 1           /* x0 = warm_basis (interior values used) */
+} msfem_warm_start;
+
+typedef struct msfem_coef_desc {
+  int32_t kind;                 /* msfem_coef_kind */
+  int32_t ncomp;                /* TABULATED only */
+  double params[8];
+  const double *qp_values;      /* TABULATED */
+  const int64_t *qp_offset;     /* TABULATED, per-cell offset in doubles; NULL = uniform blocks */
+  const double *modes;          /* FOURIER [n_fields][n_modes][5] */
+  int32_t n_modes;
+  int32_t n_spheres;
+  const double *spheres;        /* SPHERES [n_spheres][4], always host memory */
+} msfem_coef_desc;
+
+typedef struct msfem_batch_desc {
+  int32_t dim;                  /* 2 or 3 */
+  int32_t n_cells;
+  int32_t n_fine;               /* N for all cells when n_fine_per_cell == NULL */
+  int32_t precision;            /* msfem_precision */
+  const double *corners;        /* [n_cells][2^dim][dim] */
+  const int32_t *n_fine_per_cell; /* optional, [n_cells] (uneven local refinement) */
+  msfem_coef_desc coef;
+  double f_value;               /* constant right-hand side f (reference: 2.0) */
+  double tol;                   /* relative l2 residual tolerance ||b-Ax||/||b|| */
+  int32_t maxit;                /* CG iteration cap per solve (reference: 1000) */
+  int32_t memory;               /* msfem_memory */
+  int32_t warm_start;           /* msfem_warm_start */
+  int32_t check_interval;       /* residual-norm check every k iterations, 0 = tuned default */
+  const double *warm_basis;     /* [n_cells][2^dim][n^dim], WARM_USER only; uneven N: cell blocks of 2^d (N_c+1)^d */
+} msfem_batch_desc;
+
+typedef struct msfem_stats {
+  int64_t solves;               /* 2^d * n_cells */
+  int64_t cells_converged;
+  int64_t cells_failed;
+  int64_t iterations_total;     /* CG iterations summed over solves (inner FP32 ones in MIXED) */
+  int32_t iterations_max;
+  int32_t refinements_max;      /* MIXED: outer FP64 refinement steps, max over cells */
+  double max_rel_residual;      /* true FP64 ||b - A phi||/||b||, max over solves */
+  double kernel_ms;             /* device time of the solve kernel(s) */
+  double total_ms;              /* wall time of the call */
+  int32_t kernel_launches;      /* kernels this call launched */
+  int32_t ctas_per_sm;
+  int64_t h2d_bytes;
+  int64_t d2h_bytes;
+} msfem_stats;
+
+typedef struct msfem_handle msfem_handle;
+
+/* Create a handle on CUDA device `device`.  Fails with MSFEM_ERR_NO_DEVICE
+ * when the device is absent or not an sm_103 part. */
+int msfem_create(msfem_handle **handle, int device);
+
+/* Release all device buffers, streams and graphs of the handle. */
+int msfem_destroy(msfem_handle *handle);
+
+/* Launch on this stream (a cudaStream_t) instead of the handle's own.  NULL
+ * restores the handle's stream. */
+int msfem_set_stream(msfem_handle *handle, void *cuda_stream);
+
+/* Compute the multiscale basis of a batch of coarse cells.
+ *   M            [n_cells][2^d][2^d]   coarse element matrices
+ *   F            [n_cells][2^d]        coarse element loads
+ *   basis        [n_cells][2^d][n^d]   optional (NULL): basis values at the fine
+ *                nodes (uneven N: cell blocks of 2^d (N_c+1)^d, in cell order)
+ *   cell_status  [n_cells]             optional, msfem_cell_status
+ *   iterations   [n_cells][2^d]        optional, CG iterations per solve
+ *   stats        optional
+ * Output pointers follow desc->memory.  Returns MSFEM_ERR_NOT_CONVERGED when
+ * some cell failed (its status says why); outputs of the other cells are valid. */
+int msfem_run_batch(msfem_handle *handle, const msfem_batch_desc *desc,
+                    double *M, double *F, double *basis,
+                    int32_t *cell_status, int32_t *iterations,
+                    msfem_stats *stats);
+
+/* Evaluate the coefficient of desc->coef (any analytic kind) at the Gauss
+ * points of every fine cell of the batch, in the TABULATED layout, on the
+ * device.  qp_values is a device pointer when desc->memory is DEVICE. */
+int msfem_tabulate_coefficient(msfem_handle *handle,
+                               const msfem_batch_desc *desc,
+                               int32_t ncomp, double *qp_values);
+
+/* Number of doubles msfem_tabulate_coefficient writes for this batch. */
+int64_t msfem_tabulated_size(const msfem_batch_desc *desc, int32_t ncomp);
+
+/* Message of the last failing call on this thread. */
+int msfem_last_error(char *buf, size_t len);
+
+/* Library version string. */
+const char *msfem_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MSFEM_GPU_H_ */

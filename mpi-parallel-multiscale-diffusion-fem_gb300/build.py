@@ -1,0 +1,86 @@
+"""Build of the package's native libraries (in-tree, no cmake).
+
+  lib/libmsfem_gpu.so   CUDA kernels + C-ABI, nvcc for sm_103a only
+  lib/libmsfem_host.so  C++ host layer mirroring the reference's
+                        DiffusionProblemBasis / coefficient interfaces,
+                        linked against libmsfem_gpu.so
+"""
+import os
+import subprocess
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_REPO = os.path.dirname(_HERE)
+INCLUDE = os.path.join(_REPO, "include")
+CSRC = os.path.join(_HERE, "csrc")
+HOST = os.path.join(_HERE, "host")
+LIB_DIR = os.path.join(_HERE, "lib")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-shared",
+              "--expt-relaxed-constexpr"]
+
+
+def _nvcc():
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if cand and (os.path.sep not in cand or os.path.exists(cand)):
+            return cand
+    return "nvcc"
+
+
+def _run(cmd, quiet):
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError("build failed: " + " ".join(cmd) + "\n" + res.stdout + res.stderr)
+    if not quiet and res.stderr.strip():
+        print(res.stderr)
+    return res
+
+
+def _stale(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
+
+
+def _sources(folder, exts):
+    out = []
+    for root, _, files in os.walk(folder):
+        for f in files:
+            if f.endswith(exts):
+                out.append(os.path.join(root, f))
+    return sorted(out)
+
+
+def build_gpu(force=False, quiet=True, extra=()):
+    os.makedirs(LIB_DIR, exist_ok=True)
+    target = os.path.join(LIB_DIR, "libmsfem_gpu.so")
+    deps = _sources(CSRC, (".cu", ".cuh", ".h")) + [os.path.join(INCLUDE, "msfem_gpu.h")]
+    if force or _stale(target, deps):
+        cmd = [_nvcc(), *ARCH, *NVCC_FLAGS, *extra, "-I", INCLUDE, "-I", CSRC,
+               "-o", target + ".tmp", os.path.join(CSRC, "msfem_gpu.cu")]
+        _run(cmd, quiet)
+        os.replace(target + ".tmp", target)
+    return target
+
+
+def build_host(force=False, quiet=True):
+    """C++ mirror of the reference interfaces (no CUDA code; links the GPU lib)."""
+    src = os.path.join(HOST, "msfem_host.cpp")
+    if not os.path.exists(src):
+        return None
+    os.makedirs(LIB_DIR, exist_ok=True)
+    target = os.path.join(LIB_DIR, "libmsfem_host.so")
+    deps = _sources(HOST, (".cpp", ".hpp", ".h")) + [os.path.join(INCLUDE, "msfem_gpu.h"),
+                                                      os.path.join(LIB_DIR, "libmsfem_gpu.so")]
+    if force or _stale(target, deps):
+        cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-I", INCLUDE, "-I", HOST,
+               "-o", target + ".tmp", src, "-L", LIB_DIR, "-lmsfem_gpu",
+               "-Wl,-rpath,$ORIGIN"]
+        _run(cmd, quiet)
+        os.replace(target + ".tmp", target)
+    return target
+
+
+def build_all(force=False, quiet=True):
+    return [build_gpu(force, quiet), build_host(force, quiet)]

@@ -1,0 +1,798 @@
+// msfem_gpu.cu -- libmsfem_gpu.so: C-ABI (include/msfem_gpu.h) over the
+// sm_103a multiscale-basis kernels.
+//
+// Replaces, per batch of coarse cells, DiffusionProblemBasis<dim>::run()
+// (include/base/diffusion_problem_basis.tpp:438-474) as called by
+// DiffusionProblemMultiscale<dim>::initialize_and_compute_basis
+// (include/base/diffusion_problem_ms.tpp:81-87).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "msfem_common.cuh"
+#include "msfem_kernel2d.cuh"
+#include "msfem_kernel3d.cuh"
+#include "msfem_gpu.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string &msg) {
+  g_last_error = msg;
+  return code;
+}
+
+#define MSFEM_CUDA(call)                                                        \
+  do {                                                                          \
+    cudaError_t e_ = (call);                                                    \
+    if (e_ != cudaSuccess)                                                      \
+      return fail(MSFEM_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+struct DevBuf {
+  void *ptr = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+    size_t want = std::max<size_t>(bytes, 256);
+    cudaError_t e = cudaMalloc(&ptr, want);
+    if (e == cudaSuccess) cap = want;
+    return e;
+  }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+  }
+  template <typename T> T *as() const { return static_cast<T *>(ptr); }
+};
+
+}  // namespace
+
+struct msfem_handle {
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // inputs staged from the host / internal scratch
+  DevBuf corners, nfine, order, queue, qp, qpoff, warm, boff, modes, spheres, sgrid_start, sgrid_ids;
+  // outputs staged to the host / internal
+  DevBuf M, F, basis, status, iters, relres, refine;
+};
+
+namespace msfem {
+
+// ---------------------------------------------------------------------------
+// Coefficient tabulation at the QGauss(2) points (analytic kinds), layout
+// [comp][q][fine cell] per cell.  One CTA per coarse cell.
+// ---------------------------------------------------------------------------
+struct TabParams {
+  int dim, n_cells, n_fine_uniform, kind, ncomp, n_modes;
+  const double *corners;
+  const int32_t *n_fine;
+  const int64_t *offset;
+  double cparams[8];
+  const double *modes;      // [fields][n_modes][5]
+  const double *spheres;    // [n][4]
+  const int32_t *sg_start;  // sphere hash grid
+  const int32_t *sg_ids;
+  int sg_G;
+  double sg_h;
+  double *out;
+};
+
+__device__ double fourier_field(const TabParams &t, int f, const double *x) {
+  double g = 0.0;
+  const double *md = t.modes + (int64_t)f * t.n_modes * 5;
+  for (int m = 0; m < t.n_modes; ++m) {
+    const double ph = md[5 * m] * x[0] + md[5 * m + 1] * x[1] +
+                      (t.dim == 3 ? md[5 * m + 2] * x[2] : 0.0) + md[5 * m + 4];
+    g = fma(md[5 * m + 3], cos(ph), g);
+  }
+  return g;
+}
+
+__device__ bool inside_sphere(const TabParams &t, const double *x) {
+  int idx[3] = {0, 0, 0};
+  for (int a = 0; a < t.dim; ++a) {
+    int i = (int)floor(x[a] / t.sg_h);
+    idx[a] = min(max(i, 0), t.sg_G - 1);
+  }
+  const int g = idx[0] + t.sg_G * (idx[1] + (t.dim == 3 ? t.sg_G * idx[2] : 0));
+  for (int e = t.sg_start[g]; e < t.sg_start[g + 1]; ++e) {
+    const double *s = t.spheres + 4 * t.sg_ids[e];
+    double d2 = 0.0;
+    for (int a = 0; a < t.dim; ++a) d2 += (x[a] - s[a]) * (x[a] - s[a]);
+    if (d2 <= s[3] * s[3]) return true;
+  }
+  return false;
+}
+
+__global__ void tabulate_kernel(const TabParams t) {
+  const int cell = blockIdx.x;
+  if (cell >= t.n_cells) return;
+  const int dim = t.dim, nv = 1 << dim;
+  const int N = t.n_fine ? t.n_fine[cell] : t.n_fine_uniform;
+  int nfc = N * N;
+  if (dim == 3) nfc *= N;
+  const double *cr = t.corners + (int64_t)cell * nv * dim;
+  double *out = t.out + (t.offset ? t.offset[cell] : (int64_t)cell * t.ncomp * nv * nfc);
+  const double invN = 1.0 / N;
+  for (int fc = threadIdx.x; fc < nfc; fc += blockDim.x) {
+    const int cx = fc % N, cy = (fc / N) % N, cz = dim == 3 ? fc / (N * N) : 0;
+    for (int q = 0; q < nv; ++q) {
+      double tt[3];
+      tt[0] = (cx + gauss2(q & 1)) * invN;
+      tt[1] = (cy + gauss2((q >> 1) & 1)) * invN;
+      tt[2] = (cz + gauss2((q >> 2) & 1)) * invN;
+      double x[3] = {0.0, 0.0, 0.0};
+      for (int v = 0; v < nv; ++v) {
+        double w = 1.0;
+        for (int a = 0; a < dim; ++a) w *= ((v >> a) & 1) ? tt[a] : 1.0 - tt[a];
+        for (int a = 0; a < dim; ++a) x[a] += w * cr[v * dim + a];
+      }
+      double comp[6] = {0, 0, 0, 0, 0, 0};
+      double a_scalar = 0.0;
+      bool scalar = true;
+      switch (t.kind) {
+      case MSFEM_COEF_REFERENCE: {
+        const double c = 1.0 * (1.0 - 0.9999 * (0.5 * sin(2 * kPiD * 57 * x[0]) +
+                                                0.5 * sin(2 * kPiD * 57 * x[1])));
+        for (int k = 0; k < (dim == 2 ? 3 : 6); ++k) comp[k] = c * t.cparams[k];
+        scalar = false;
+        break;
+      }
+      case MSFEM_COEF_SINSIN: {
+        const double ie = 2.0 / t.cparams[1];
+        double s = sinpi(x[0] * ie) * sinpi(x[1] * ie);
+        if (dim == 3) s *= sinpi(x[2] * ie);
+        a_scalar = 1.0 + t.cparams[0] * s;
+        break;
+      }
+      case MSFEM_COEF_FOURIER: {
+        if (dim == 2) {
+          const double g1 = fourier_field(t, 0, x), g2 = fourier_field(t, 1, x);
+          const double th = fourier_field(t, 2, x);
+          double sn, cn;
+          sincos(th, &sn, &cn);
+          const double e1 = exp(g1), e2 = exp(g2);
+          // R diag(e1,e2) R^T, R = [[c,-s],[s,c]]
+          comp[0] = cn * cn * e1 + sn * sn * e2;
+          comp[1] = cn * sn * (e1 - e2);
+          comp[2] = sn * sn * e1 + cn * cn * e2;
+          scalar = false;
+        } else {
+          a_scalar = exp(fourier_field(t, 0, x));
+        }
+        break;
+      }
+      case MSFEM_COEF_SPHERES:
+        a_scalar = inside_sphere(t, x) ? t.cparams[0] : 1.0;
+        break;
+      default:  // CONSTANT
+        for (int k = 0; k < (dim == 2 ? 3 : 6); ++k) comp[k] = t.cparams[k];
+        scalar = false;
+        break;
+      }
+      if (scalar) {
+        if (t.ncomp == 1) {
+          comp[0] = a_scalar;
+        } else if (dim == 2) {
+          comp[0] = a_scalar; comp[1] = 0.0; comp[2] = a_scalar;
+        } else {
+          comp[0] = a_scalar; comp[1] = comp[2] = 0.0; comp[3] = a_scalar; comp[4] = 0.0; comp[5] = a_scalar;
+        }
+      }
+      // ncomp == 1 with a tensor kind keeps a11 (caller's choice)
+      for (int k = 0; k < t.ncomp; ++k) out[((int64_t)k * nv + q) * nfc + fc] = comp[k];
+    }
+  }
+}
+
+}  // namespace msfem
+
+namespace {
+
+using msfem::KernelParams;
+
+int ipow(int a, int e) {
+  int r = 1;
+  while (e-- > 0) r *= a;
+  return r;
+}
+
+int cell_N(const msfem_batch_desc *d, const std::vector<int32_t> &nf, int c) {
+  return d->n_fine_per_cell ? nf[c] : d->n_fine;
+}
+
+// Reference MatrixCoeff rotation products R R^T (matrix_coeff.tpp:17-41).
+void reference_rrt(int dim, double *out) {
+  const double pi_d = msfem::kPiD;
+  const double al = pi_d / 3, be = pi_d / 6, ga = pi_d / 4;
+  double R[9];
+  if (dim == 2) {
+    R[0] = cos(al); R[1] = sin(al); R[2] = -sin(al); R[3] = cos(al);
+    out[0] = R[0] * R[0] + R[1] * R[1];
+    out[1] = R[0] * R[2] + R[1] * R[3];
+    out[2] = R[2] * R[2] + R[3] * R[3];
+  } else {
+    R[0] = cos(al) * cos(ga) - sin(al) * cos(be) * sin(ga);
+    R[1] = -cos(al) * sin(ga) - sin(al) * cos(be) * cos(ga);
+    R[2] = sin(al) * sin(be);
+    R[3] = sin(al) * cos(ga) + cos(al) * cos(be) * sin(ga);
+    R[4] = -sin(al) * sin(ga) + cos(al) * cos(be) * cos(ga);
+    R[5] = -cos(al) * sin(be);
+    R[6] = sin(be) * sin(ga);
+    R[7] = sin(be) * cos(ga);
+    R[8] = cos(be);
+    auto rr = [&](int i, int j) {
+      return R[3 * i] * R[3 * j] + R[3 * i + 1] * R[3 * j + 1] + R[3 * i + 2] * R[3 * j + 2];
+    };
+    out[0] = rr(0, 0); out[1] = rr(0, 1); out[2] = rr(0, 2);
+    out[3] = rr(1, 1); out[4] = rr(1, 2); out[5] = rr(2, 2);
+  }
+}
+
+template <typename T>
+int upload(msfem_handle *h, DevBuf &buf, const T *src, size_t count, bool device,
+           const T **dst, int64_t *h2d) {
+  if (count == 0) {
+    *dst = nullptr;
+    return MSFEM_OK;
+  }
+  if (device) {
+    *dst = src;
+    return MSFEM_OK;
+  }
+  MSFEM_CUDA(buf.ensure(count * sizeof(T)));
+  MSFEM_CUDA(cudaMemcpyAsync(buf.ptr, src, count * sizeof(T), cudaMemcpyHostToDevice, h->stream));
+  *h2d += (int64_t)(count * sizeof(T));
+  *dst = buf.as<T>();
+  return MSFEM_OK;
+}
+
+// Kernel selection.  NMAX is the largest N of the batch rounded up to a
+// compiled size class.
+struct Launch {
+  const void *fn;
+  int nt;
+  size_t smem;
+};
+
+template <int NMAX, int NT, bool MIXED>
+Launch make2d() {
+  return Launch{(const void *)msfem::msfem2d_kernel<NMAX, NT, MIXED>, NT,
+                msfem::Smem2D<NMAX>::bytes(MIXED)};
+}
+
+int pick2d(int nmax, bool mixed, Launch *l) {
+  if (nmax <= 16) *l = mixed ? make2d<16, 256, true>() : make2d<16, 128, false>();
+  else if (nmax <= 32) *l = mixed ? make2d<32, 512, true>() : make2d<32, 256, false>();
+  else return -1;
+  return 0;
+}
+
+int pick3d(int nmax, bool mixed, Launch *l) {
+  return msfem::pick3d_kernel(nmax, mixed, &l->fn, &l->nt, &l->smem);
+}
+
+// Sphere hash grid (uniform cells of width >= 2 r_max; each sphere listed in
+// every grid cell its bounding box touches).
+void build_sphere_grid(int dim, const double *sp, int n, std::vector<int32_t> &start,
+                       std::vector<int32_t> &ids, int *Gout, double *hout) {
+  double rmax = 0.0;
+  for (int s = 0; s < n; ++s) rmax = std::max(rmax, sp[4 * s + 3]);
+  double h = std::max(2.0 * rmax, 1e-3);
+  int G = std::min(256, std::max(1, (int)std::ceil(1.0 / h)));
+  h = 1.0 / G;
+  const int ncell = ipow(G, dim);
+  std::vector<int32_t> cnt(ncell + 1, 0);
+  for (int pass = 0; pass < 2; ++pass) {
+    for (int s = 0; s < n; ++s) {
+      int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+      for (int a = 0; a < dim; ++a) {
+        const double c = sp[4 * s + a], r = sp[4 * s + 3];
+        lo[a] = std::max(0, (int)std::floor((c - r) / h));
+        hi[a] = std::min(G - 1, (int)std::floor((c + r) / h));
+      }
+      for (int k = lo[2]; k <= hi[2]; ++k)
+        for (int j = lo[1]; j <= hi[1]; ++j)
+          for (int i = lo[0]; i <= hi[0]; ++i) {
+            const int g = i + G * (j + (dim == 3 ? G * k : 0));
+            if (pass == 0) cnt[g + 1]++;
+            else ids[cnt[g]++] = s;
+          }
+    }
+    if (pass == 0) {
+      for (int g = 0; g < ncell; ++g) cnt[g + 1] += cnt[g];
+      start = cnt;
+      ids.assign(std::max<int32_t>(1, cnt[ncell]), 0);
+    }
+  }
+  *Gout = G;
+  *hout = h;
+}
+
+int validate(const msfem_batch_desc *d) {
+  if (!d) return fail(MSFEM_ERR_INVALID_ARG, "descriptor is NULL");
+  if (d->dim != 2 && d->dim != 3) return fail(MSFEM_ERR_INVALID_ARG, "dim must be 2 or 3");
+  if (d->n_cells < 0) return fail(MSFEM_ERR_INVALID_ARG, "n_cells < 0");
+  if (d->n_cells > 0 && !d->corners) return fail(MSFEM_ERR_INVALID_ARG, "corners is NULL");
+  if (!d->n_fine_per_cell) {
+    const int nmax = d->dim == 2 ? MSFEM_MAX_N_2D : MSFEM_MAX_N_3D;
+    if (d->n_fine < 1 || d->n_fine > nmax)
+      return fail(MSFEM_ERR_INVALID_ARG, "n_fine out of range [1, " + std::to_string(nmax) + "]");
+  }
+  if (d->precision != MSFEM_PREC_FP64 && d->precision != MSFEM_PREC_MIXED)
+    return fail(MSFEM_ERR_INVALID_ARG, "unknown precision");
+  if (d->memory != MSFEM_MEM_HOST && d->memory != MSFEM_MEM_DEVICE)
+    return fail(MSFEM_ERR_INVALID_ARG, "unknown memory kind");
+  if (!(d->tol > 0.0) || !std::isfinite(d->tol)) return fail(MSFEM_ERR_INVALID_ARG, "tol must be > 0");
+  if (d->maxit < 1) return fail(MSFEM_ERR_INVALID_ARG, "maxit must be >= 1");
+  if (d->check_interval < 0) return fail(MSFEM_ERR_INVALID_ARG, "check_interval < 0");
+  if (d->warm_start != MSFEM_WARM_NONE && d->warm_start != MSFEM_WARM_USER)
+    return fail(MSFEM_ERR_INVALID_ARG, "unknown warm_start");
+  if (d->warm_start == MSFEM_WARM_USER && d->n_cells > 0 && !d->warm_basis)
+    return fail(MSFEM_ERR_INVALID_ARG, "warm_basis is NULL");
+  const msfem_coef_desc &c = d->coef;
+  switch (c.kind) {
+  case MSFEM_COEF_CONSTANT:
+  case MSFEM_COEF_REFERENCE:
+  case MSFEM_COEF_SINSIN:
+    break;
+  case MSFEM_COEF_FOURIER:
+    if (!c.modes || c.n_modes < 1) return fail(MSFEM_ERR_INVALID_ARG, "FOURIER needs modes");
+    break;
+  case MSFEM_COEF_SPHERES:
+    if (c.n_spheres < 0 || (c.n_spheres > 0 && !c.spheres))
+      return fail(MSFEM_ERR_INVALID_ARG, "SPHERES needs spheres");
+    break;
+  case MSFEM_COEF_TABULATED: {
+    const int full = d->dim == 2 ? 3 : 6;
+    if (c.ncomp != 1 && c.ncomp != full)
+      return fail(MSFEM_ERR_INVALID_ARG, "TABULATED ncomp must be 1 or d(d+1)/2");
+    if (d->n_cells > 0 && !c.qp_values) return fail(MSFEM_ERR_INVALID_ARG, "qp_values is NULL");
+    break;
+  }
+  default:
+    return fail(MSFEM_ERR_INVALID_ARG, "unknown coefficient kind");
+  }
+  if (c.kind == MSFEM_COEF_SINSIN && !(c.params[1] != 0.0))
+    return fail(MSFEM_ERR_INVALID_ARG, "SINSIN eps must be nonzero");
+  return MSFEM_OK;
+}
+
+// Fill the per-cell N vector on the host (copying it from the device when needed).
+int host_nfine(msfem_handle *h, const msfem_batch_desc *d, std::vector<int32_t> &nf) {
+  nf.clear();
+  if (!d->n_fine_per_cell) return MSFEM_OK;
+  nf.resize(d->n_cells);
+  if (d->memory == MSFEM_MEM_DEVICE) {
+    MSFEM_CUDA(cudaMemcpyAsync(nf.data(), d->n_fine_per_cell, sizeof(int32_t) * d->n_cells,
+                               cudaMemcpyDeviceToHost, h->stream));
+    MSFEM_CUDA(cudaStreamSynchronize(h->stream));
+  } else {
+    std::memcpy(nf.data(), d->n_fine_per_cell, sizeof(int32_t) * d->n_cells);
+  }
+  const int nmax = d->dim == 2 ? MSFEM_MAX_N_2D : MSFEM_MAX_N_3D;
+  for (int c = 0; c < d->n_cells; ++c)
+    if (nf[c] < 1 || nf[c] > nmax)
+      return fail(MSFEM_ERR_INVALID_ARG, "n_fine_per_cell[" + std::to_string(c) + "] out of range");
+  return MSFEM_OK;
+}
+
+// Evaluate an analytic coefficient into a device TABULATED buffer.
+int run_tabulate(msfem_handle *h, const msfem_batch_desc *d, const std::vector<int32_t> &nf,
+                 const double *corners_dev, const int32_t *nfine_dev, int ncomp, double *out_dev,
+                 const int64_t *offsets_dev, int64_t *h2d, int *launches) {
+  msfem::TabParams t{};
+  t.dim = d->dim;
+  t.n_cells = d->n_cells;
+  t.n_fine_uniform = d->n_fine;
+  t.kind = d->coef.kind;
+  t.ncomp = ncomp;
+  t.corners = corners_dev;
+  t.n_fine = nfine_dev;
+  t.offset = offsets_dev;
+  t.out = out_dev;
+  for (int k = 0; k < 8; ++k) t.cparams[k] = d->coef.params[k];
+  if (t.kind == MSFEM_COEF_REFERENCE) reference_rrt(d->dim, t.cparams);
+  const bool dev = d->memory == MSFEM_MEM_DEVICE;
+  if (t.kind == MSFEM_COEF_FOURIER) {
+    const int nf_fields = d->dim == 2 ? 3 : 1;
+    const double *m = nullptr;
+    int rc = upload<double>(h, h->modes, d->coef.modes, (size_t)nf_fields * d->coef.n_modes * 5, dev, &m, h2d);
+    if (rc) return rc;
+    t.modes = m;
+    t.n_modes = d->coef.n_modes;
+  }
+  if (t.kind == MSFEM_COEF_SPHERES) {
+    std::vector<int32_t> start, ids;
+    int G = 1;
+    double hh = 1.0;
+    build_sphere_grid(d->dim, d->coef.spheres, d->coef.n_spheres, start, ids, &G, &hh);
+    const double *sp = nullptr;
+    const int32_t *st = nullptr, *id = nullptr;
+    int rc = upload<double>(h, h->spheres, d->coef.spheres, (size_t)std::max(1, d->coef.n_spheres) * 4,
+                            false, &sp, h2d);
+    if (rc) return rc;
+    rc = upload<int32_t>(h, h->sgrid_start, start.data(), start.size(), false, &st, h2d);
+    if (rc) return rc;
+    rc = upload<int32_t>(h, h->sgrid_ids, ids.data(), ids.size(), false, &id, h2d);
+    if (rc) return rc;
+    t.spheres = sp;
+    t.sg_start = st;
+    t.sg_ids = id;
+    t.sg_G = G;
+    t.sg_h = hh;
+  }
+  if (d->n_cells == 0) return MSFEM_OK;
+  msfem::tabulate_kernel<<<d->n_cells, 256, 0, h->stream>>>(t);
+  MSFEM_CUDA(cudaGetLastError());
+  (*launches)++;
+  (void)nf;
+  return MSFEM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *msfem_version(void) { return "msfem_gpu 0.1 (sm_103a)"; }
+
+int msfem_last_error(char *buf, size_t len) {
+  if (!buf || len == 0) return MSFEM_ERR_INVALID_ARG;
+  std::snprintf(buf, len, "%s", g_last_error.c_str());
+  return MSFEM_OK;
+}
+
+int msfem_create(msfem_handle **handle, int device) {
+  if (!handle) return fail(MSFEM_ERR_INVALID_ARG, "handle is NULL");
+  *handle = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev)
+    return fail(MSFEM_ERR_NO_DEVICE, "CUDA device " + std::to_string(device) + " not available");
+  cudaDeviceProp prop;
+  MSFEM_CUDA(cudaGetDeviceProperties(&prop, device));
+  if (prop.major != 10 || prop.minor != 3)
+    return fail(MSFEM_ERR_NO_DEVICE, std::string("device is sm_") + std::to_string(prop.major) +
+                                         std::to_string(prop.minor) + ", this build targets sm_103a");
+  MSFEM_CUDA(cudaSetDevice(device));
+  msfem_handle *h = new msfem_handle();
+  h->device = device;
+  h->sm_count = prop.multiProcessorCount;
+  if (cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess) {
+    delete h;
+    return fail(MSFEM_ERR_CUDA, "stream/event creation failed");
+  }
+  h->stream = h->own_stream;
+  *handle = h;
+  return MSFEM_OK;
+}
+
+int msfem_destroy(msfem_handle *h) {
+  if (!h) return MSFEM_OK;
+  cudaSetDevice(h->device);
+  cudaStreamSynchronize(h->stream);
+  DevBuf *bufs[] = {&h->corners, &h->nfine, &h->order, &h->queue, &h->qp, &h->qpoff, &h->warm,
+                    &h->boff, &h->modes, &h->spheres, &h->sgrid_start, &h->sgrid_ids,
+                    &h->M, &h->F, &h->basis, &h->status, &h->iters, &h->relres, &h->refine};
+  for (DevBuf *b : bufs) b->release();
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->own_stream) cudaStreamDestroy(h->own_stream);
+  delete h;
+  return MSFEM_OK;
+}
+
+int msfem_set_stream(msfem_handle *h, void *stream) {
+  if (!h) return fail(MSFEM_ERR_INVALID_ARG, "handle is NULL");
+  h->stream = stream ? static_cast<cudaStream_t>(stream) : h->own_stream;
+  return MSFEM_OK;
+}
+
+int64_t msfem_tabulated_size(const msfem_batch_desc *d, int32_t ncomp) {
+  if (!d || (d->dim != 2 && d->dim != 3) || d->n_cells < 0) return -1;
+  const int nq = 1 << d->dim;
+  if (!d->n_fine_per_cell) return (int64_t)d->n_cells * ncomp * nq * ipow(d->n_fine, d->dim);
+  if (d->memory == MSFEM_MEM_DEVICE) return -1;  // sizes live on the device
+  int64_t s = 0;
+  for (int c = 0; c < d->n_cells; ++c) s += (int64_t)ncomp * nq * ipow(d->n_fine_per_cell[c], d->dim);
+  return s;
+}
+
+int msfem_tabulate_coefficient(msfem_handle *h, const msfem_batch_desc *d, int32_t ncomp,
+                               double *qp_values) {
+  if (!h) return fail(MSFEM_ERR_INVALID_ARG, "handle is NULL");
+  int rc = validate(d);
+  if (rc) return rc;
+  if (d->coef.kind == MSFEM_COEF_TABULATED)
+    return fail(MSFEM_ERR_INVALID_ARG, "coefficient is already tabulated");
+  const int full = d->dim == 2 ? 3 : 6;
+  if (ncomp != 1 && ncomp != full) return fail(MSFEM_ERR_INVALID_ARG, "ncomp must be 1 or d(d+1)/2");
+  if (d->n_cells > 0 && !qp_values) return fail(MSFEM_ERR_INVALID_ARG, "qp_values is NULL");
+  MSFEM_CUDA(cudaSetDevice(h->device));
+  std::vector<int32_t> nf;
+  if ((rc = host_nfine(h, d, nf))) return rc;
+  const bool dev = d->memory == MSFEM_MEM_DEVICE;
+  const int nv = 1 << d->dim;
+  int64_t h2d = 0;
+  int launches = 0;
+  const double *corners = nullptr;
+  const int32_t *nfd = nullptr;
+  if ((rc = upload<double>(h, h->corners, d->corners, (size_t)d->n_cells * nv * d->dim, dev, &corners, &h2d))) return rc;
+  if (d->n_fine_per_cell)
+    if ((rc = upload<int32_t>(h, h->nfine, d->n_fine_per_cell, (size_t)d->n_cells, dev, &nfd, &h2d))) return rc;
+  std::vector<int64_t> off;
+  const int64_t *offd = nullptr;
+  int64_t total = (int64_t)d->n_cells * ncomp * nv * ipow(d->n_fine, d->dim);
+  if (d->n_fine_per_cell) {
+    off.resize(d->n_cells);
+    total = 0;
+    for (int c = 0; c < d->n_cells; ++c) {
+      off[c] = total;
+      total += (int64_t)ncomp * nv * ipow(nf[c], d->dim);
+    }
+    if ((rc = upload<int64_t>(h, h->qpoff, off.data(), off.size(), false, &offd, &h2d))) return rc;
+  }
+  double *out = qp_values;
+  if (!dev) {
+    MSFEM_CUDA(h->qp.ensure(sizeof(double) * std::max<int64_t>(1, total)));
+    out = h->qp.as<double>();
+  }
+  if ((rc = run_tabulate(h, d, nf, corners, nfd, ncomp, out, offd, &h2d, &launches))) return rc;
+  if (!dev && total > 0)
+    MSFEM_CUDA(cudaMemcpyAsync(qp_values, out, sizeof(double) * total, cudaMemcpyDeviceToHost, h->stream));
+  MSFEM_CUDA(cudaStreamSynchronize(h->stream));
+  return MSFEM_OK;
+}
+
+int msfem_run_batch(msfem_handle *h, const msfem_batch_desc *d, double *M, double *F,
+                    double *basis, int32_t *cell_status, int32_t *iterations,
+                    msfem_stats *stats) {
+  const auto t_start = std::chrono::steady_clock::now();
+  if (!h) return fail(MSFEM_ERR_INVALID_ARG, "handle is NULL");
+  int rc = validate(d);
+  if (rc) return rc;
+  if (d->n_cells > 0 && (!M || !F)) return fail(MSFEM_ERR_INVALID_ARG, "M and F are required");
+  MSFEM_CUDA(cudaSetDevice(h->device));
+  const int dim = d->dim, nv = 1 << dim, nc = d->n_cells;
+  const bool dev = d->memory == MSFEM_MEM_DEVICE;
+  const bool mixed = d->precision == MSFEM_PREC_MIXED;
+  std::vector<int32_t> nf;
+  if ((rc = host_nfine(h, d, nf))) return rc;
+  int nmax = d->n_fine;
+  if (d->n_fine_per_cell) {
+    nmax = 1;
+    for (int c = 0; c < nc; ++c) nmax = std::max(nmax, nf[c]);
+  }
+  Launch L{};
+  if ((dim == 2 ? pick2d(nmax, mixed, &L) : pick3d(nmax, mixed, &L)) != 0)
+    return fail(MSFEM_ERR_UNSUPPORTED, "no kernel for dim " + std::to_string(dim) + ", N " +
+                                           std::to_string(nmax));
+  int64_t h2d = 0, d2h = 0;
+  int launches = 0;
+
+  // ---- inputs
+  const double *corners = nullptr;
+  const int32_t *nfd = nullptr;
+  if ((rc = upload<double>(h, h->corners, d->corners, (size_t)nc * nv * dim, dev, &corners, &h2d))) return rc;
+  if (d->n_fine_per_cell)
+    if ((rc = upload<int32_t>(h, h->nfine, d->n_fine_per_cell, (size_t)nc, dev, &nfd, &h2d))) return rc;
+  // per-cell basis offsets (uneven N) and the size-sorted work queue
+  std::vector<int64_t> boff;
+  const int64_t *boffd = nullptr;
+  const int32_t *orderd = nullptr;
+  int64_t basis_total = (int64_t)nc * nv * ipow(d->n_fine + 1, dim);
+  if (d->n_fine_per_cell) {
+    boff.resize(nc);
+    basis_total = 0;
+    for (int c = 0; c < nc; ++c) {
+      boff[c] = basis_total;
+      basis_total += (int64_t)nv * ipow(nf[c] + 1, dim);
+    }
+    if ((rc = upload<int64_t>(h, h->boff, boff.data(), boff.size(), false, &boffd, &h2d))) return rc;
+    // largest cells first (counting sort on N, stable)
+    std::vector<int32_t> order(nc);
+    std::vector<int> cnt(MSFEM_MAX_N_2D + 2, 0);
+    for (int c = 0; c < nc; ++c) cnt[nf[c]]++;
+    std::vector<int> pos(MSFEM_MAX_N_2D + 2, 0);
+    int acc = 0;
+    for (int v = MSFEM_MAX_N_2D; v >= 1; --v) { pos[v] = acc; acc += cnt[v]; }
+    for (int c = 0; c < nc; ++c) order[pos[nf[c]]++] = c;
+    if ((rc = upload<int32_t>(h, h->order, order.data(), order.size(), false, &orderd, &h2d))) return rc;
+  }
+  // coefficient
+  KernelParams p{};
+  p.dim = dim;
+  p.n_cells = nc;
+  p.n_fine_uniform = d->n_fine;
+  p.corners = corners;
+  p.n_fine = nfd;
+  p.order = orderd;
+  p.f_value = d->f_value;
+  p.tol = d->tol;
+  p.maxit = d->maxit;
+  p.check_interval = d->check_interval;
+  p.inner_tol = 1e-4f;
+  p.inner_maxit = std::max(1, std::min(d->maxit, 1000));
+  p.max_refine = 40;
+  p.coef_kind = d->coef.kind;
+  p.ncomp = d->coef.ncomp;
+  for (int k = 0; k < 8; ++k) p.cparams[k] = d->coef.params[k];
+  if (p.coef_kind == MSFEM_COEF_REFERENCE) reference_rrt(dim, p.cparams);
+  if (d->coef.kind == MSFEM_COEF_TABULATED) {
+    int64_t total = 0;
+    std::vector<int64_t> off;
+    if (d->n_fine_per_cell || d->coef.qp_offset) {
+      off.resize(nc);
+      for (int c = 0; c < nc; ++c) {
+        off[c] = total;
+        total += (int64_t)d->coef.ncomp * nv * ipow(cell_N(d, nf, c), dim);
+      }
+    } else {
+      total = (int64_t)nc * d->coef.ncomp * nv * ipow(d->n_fine, dim);
+    }
+    if (d->coef.qp_offset) {
+      // caller-provided offsets: data extent = max offset + block
+      const int64_t *qo = d->coef.qp_offset;
+      std::vector<int64_t> hq(nc);
+      if (dev) {
+        MSFEM_CUDA(cudaMemcpyAsync(hq.data(), qo, sizeof(int64_t) * nc, cudaMemcpyDeviceToHost, h->stream));
+        MSFEM_CUDA(cudaStreamSynchronize(h->stream));
+      } else {
+        std::memcpy(hq.data(), qo, sizeof(int64_t) * nc);
+      }
+      total = 0;
+      for (int c = 0; c < nc; ++c)
+        total = std::max(total, hq[c] + (int64_t)d->coef.ncomp * nv * ipow(cell_N(d, nf, c), dim));
+      off = hq;
+    }
+    const double *qp = nullptr;
+    if ((rc = upload<double>(h, h->qp, d->coef.qp_values, (size_t)total, dev, &qp, &h2d))) return rc;
+    p.qp_values = qp;
+    if (!off.empty()) {
+      const int64_t *od = nullptr;
+      if ((rc = upload<int64_t>(h, h->qpoff, off.data(), off.size(), false, &od, &h2d))) return rc;
+      p.qp_offset = od;
+    }
+  } else if (d->coef.kind == MSFEM_COEF_FOURIER || d->coef.kind == MSFEM_COEF_SPHERES) {
+    // tabulate on the device first, then run the tabulated path
+    const int ncomp = (d->coef.kind == MSFEM_COEF_FOURIER && dim == 2) ? 3 : 1;
+    std::vector<int64_t> off;
+    int64_t total = (int64_t)nc * ncomp * nv * ipow(d->n_fine, dim);
+    const int64_t *od = nullptr;
+    if (d->n_fine_per_cell) {
+      off.resize(nc);
+      total = 0;
+      for (int c = 0; c < nc; ++c) {
+        off[c] = total;
+        total += (int64_t)ncomp * nv * ipow(nf[c], dim);
+      }
+      if ((rc = upload<int64_t>(h, h->qpoff, off.data(), off.size(), false, &od, &h2d))) return rc;
+    }
+    MSFEM_CUDA(h->qp.ensure(sizeof(double) * std::max<int64_t>(1, total)));
+    if ((rc = run_tabulate(h, d, nf, corners, nfd, ncomp, h->qp.as<double>(), od, &h2d, &launches))) return rc;
+    p.coef_kind = MSFEM_COEF_TABULATED;
+    p.ncomp = ncomp;
+    p.qp_values = h->qp.as<double>();
+    p.qp_offset = od;
+  }
+  if (d->warm_start == MSFEM_WARM_USER) {
+    const double *wb = nullptr;
+    if ((rc = upload<double>(h, h->warm, d->warm_basis, (size_t)basis_total, dev, &wb, &h2d))) return rc;
+    p.warm_basis = wb;
+  }
+  p.basis_offset = boffd;
+
+  // ---- outputs
+  auto out_ptr = [&](DevBuf &buf, void *user, size_t bytes) -> void * {
+    if (dev && user) return user;
+    if (buf.ensure(std::max<size_t>(bytes, 8)) != cudaSuccess) return nullptr;
+    return buf.ptr;
+  };
+  p.M = (double *)out_ptr(h->M, M, sizeof(double) * nc * nv * nv);
+  p.F = (double *)out_ptr(h->F, F, sizeof(double) * nc * nv);
+  p.status = (int32_t *)out_ptr(h->status, cell_status, sizeof(int32_t) * nc);
+  p.iters = (int32_t *)out_ptr(h->iters, iterations, sizeof(int32_t) * nc * nv);
+  p.rel_res = (double *)out_ptr(h->relres, nullptr, sizeof(double) * nc);
+  p.refinements = (int32_t *)out_ptr(h->refine, nullptr, sizeof(int32_t) * nc);
+  p.basis = basis ? (double *)out_ptr(h->basis, basis, sizeof(double) * basis_total) : nullptr;
+  if (!p.M || !p.F || !p.status || !p.iters || !p.rel_res || !p.refinements || (basis && !p.basis))
+    return fail(MSFEM_ERR_OUT_OF_MEMORY, "device output allocation failed");
+  MSFEM_CUDA(h->queue.ensure(sizeof(unsigned int)));
+  p.queue = h->queue.as<unsigned int>();
+
+  // ---- launch: persistent CTAs, size-sorted work queue
+  MSFEM_CUDA(cudaFuncSetAttribute(L.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem));
+  int per_sm = 0;
+  MSFEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, L.fn, L.nt, L.smem));
+  if (per_sm < 1) return fail(MSFEM_ERR_UNSUPPORTED, "kernel does not fit on an SM");
+  const int grid = std::max(1, std::min(nc, per_sm * h->sm_count));
+  MSFEM_CUDA(cudaMemsetAsync(p.queue, 0, sizeof(unsigned int), h->stream));
+  MSFEM_CUDA(cudaEventRecord(h->ev0, h->stream));
+  if (nc > 0) {
+    void *args[] = {&p};
+    MSFEM_CUDA(cudaLaunchKernel(L.fn, dim3(grid), dim3(L.nt), args, L.smem, h->stream));
+    launches++;
+  }
+  MSFEM_CUDA(cudaEventRecord(h->ev1, h->stream));
+
+  // ---- results
+  std::vector<int32_t> st_h, it_h, rf_h;
+  std::vector<double> rr_h;
+  const bool need_host = !dev || stats;
+  if (!dev) {
+    if (nc > 0) {
+      MSFEM_CUDA(cudaMemcpyAsync(M, p.M, sizeof(double) * nc * nv * nv, cudaMemcpyDeviceToHost, h->stream));
+      MSFEM_CUDA(cudaMemcpyAsync(F, p.F, sizeof(double) * nc * nv, cudaMemcpyDeviceToHost, h->stream));
+      d2h += sizeof(double) * (int64_t)nc * (nv * nv + nv);
+      if (basis) {
+        MSFEM_CUDA(cudaMemcpyAsync(basis, p.basis, sizeof(double) * basis_total, cudaMemcpyDeviceToHost, h->stream));
+        d2h += sizeof(double) * basis_total;
+      }
+      if (cell_status) {
+        MSFEM_CUDA(cudaMemcpyAsync(cell_status, p.status, sizeof(int32_t) * nc, cudaMemcpyDeviceToHost, h->stream));
+        d2h += sizeof(int32_t) * nc;
+      }
+      if (iterations) {
+        MSFEM_CUDA(cudaMemcpyAsync(iterations, p.iters, sizeof(int32_t) * nc * nv, cudaMemcpyDeviceToHost, h->stream));
+        d2h += sizeof(int32_t) * nc * nv;
+      }
+    }
+  }
+  int nfail = 0;
+  if (need_host && nc > 0) {
+    st_h.resize(nc);
+    it_h.resize((size_t)nc * nv);
+    rr_h.resize(nc);
+    rf_h.resize(nc);
+    MSFEM_CUDA(cudaMemcpyAsync(st_h.data(), p.status, sizeof(int32_t) * nc, cudaMemcpyDeviceToHost, h->stream));
+    MSFEM_CUDA(cudaMemcpyAsync(it_h.data(), p.iters, sizeof(int32_t) * nc * nv, cudaMemcpyDeviceToHost, h->stream));
+    MSFEM_CUDA(cudaMemcpyAsync(rr_h.data(), p.rel_res, sizeof(double) * nc, cudaMemcpyDeviceToHost, h->stream));
+    MSFEM_CUDA(cudaMemcpyAsync(rf_h.data(), p.refinements, sizeof(int32_t) * nc, cudaMemcpyDeviceToHost, h->stream));
+  }
+  if (need_host) MSFEM_CUDA(cudaStreamSynchronize(h->stream));
+  for (int c = 0; c < (int)st_h.size(); ++c) nfail += st_h[c] != MSFEM_CELL_CONVERGED;
+  if (stats) {
+    std::memset(stats, 0, sizeof(*stats));
+    stats->solves = (int64_t)nc * nv;
+    stats->cells_failed = nfail;
+    stats->cells_converged = nc - nfail;
+    int64_t tot = 0;
+    int itmax = 0, rfmax = 0;
+    double rmax = 0.0;
+    for (size_t i = 0; i < it_h.size(); ++i) { tot += it_h[i]; itmax = std::max(itmax, it_h[i]); }
+    for (int c = 0; c < (int)rr_h.size(); ++c) {
+      if (!(rr_h[c] <= rmax)) rmax = rr_h[c];  // NaN propagates
+      rfmax = std::max(rfmax, rf_h[c]);
+    }
+    stats->iterations_total = tot;
+    stats->iterations_max = itmax;
+    stats->refinements_max = rfmax;
+    stats->max_rel_residual = rmax;
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, h->ev0, h->ev1) == cudaSuccess) stats->kernel_ms = ms;
+    stats->kernel_launches = launches;
+    stats->ctas_per_sm = per_sm;
+    stats->h2d_bytes = h2d;
+    stats->d2h_bytes = d2h;
+    stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
+  }
+  if (nfail) return fail(MSFEM_ERR_NOT_CONVERGED, std::to_string(nfail) + " cell(s) failed; see cell_status");
+  return MSFEM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,150 @@
+"""Python front-end of libmsfem_gpu.so: fills msfem_batch_desc from a problem
+dict (see workloads.py) and calls the C-ABI.  The numerical work happens only
+in the CUDA library; this module never computes a basis itself."""
+import ctypes
+
+import numpy as np
+
+from . import _abi
+
+PRECISION = {"fp64": _abi.PREC_FP64, "mixed": _abi.PREC_MIXED}
+
+
+def _ptr(a):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+class Engine:
+    """One handle = one GPU (reference: one MPI rank's DiffusionProblemBasis objects)."""
+
+    def __init__(self, device=0, lib=None):
+        self.lib = lib or _abi.load()
+        h = ctypes.c_void_p()
+        rc = self.lib.msfem_create(ctypes.byref(h), device)
+        if rc != _abi.OK:
+            raise _abi.MsfemError(rc, _abi.last_error(self.lib))
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            self.lib.msfem_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_handle):
+        rc = self.lib.msfem_set_stream(self.handle, ctypes.c_void_p(stream_handle or 0))
+        if rc != _abi.OK:
+            raise _abi.MsfemError(rc, _abi.last_error(self.lib))
+
+    # -- descriptor -------------------------------------------------------
+    @staticmethod
+    def make_desc(problem, precision="fp64", tol=1e-10, maxit=1000, check_interval=0,
+                  warm_basis=None, memory=_abi.MEM_HOST, keep=None):
+        """msfem_batch_desc for host numpy data (memory=HOST).  `keep`
+        collects the arrays whose buffers the descriptor points to."""
+        keep = [] if keep is None else keep
+        d = _abi.BatchDesc()
+        d.dim = problem["dim"]
+        corners = np.ascontiguousarray(problem["corners"], dtype=np.float64)
+        keep.append(corners)
+        d.n_cells = corners.shape[0]
+        d.n_fine = int(problem.get("n_fine", 1))
+        d.precision = PRECISION[precision] if isinstance(precision, str) else int(precision)
+        d.corners = _ptr(corners)
+        if "n_fine_per_cell" in problem:
+            nf = np.ascontiguousarray(problem["n_fine_per_cell"], dtype=np.int32)
+            keep.append(nf)
+            d.n_fine_per_cell = _ptr(nf)
+        c = problem["coef"]
+        d.coef.kind = int(c["kind"])
+        d.coef.ncomp = int(c.get("ncomp", 0))
+        for i, v in enumerate(c.get("params", [])):
+            d.coef.params[i] = float(v)
+        if c.get("qp_values") is not None:
+            qv = np.ascontiguousarray(c["qp_values"], dtype=np.float64)
+            keep.append(qv)
+            d.coef.qp_values = _ptr(qv)
+        if c.get("qp_offset") is not None:
+            qo = np.ascontiguousarray(c["qp_offset"], dtype=np.int64)
+            keep.append(qo)
+            d.coef.qp_offset = _ptr(qo)
+        if c.get("modes") is not None:
+            md = np.ascontiguousarray(c["modes"], dtype=np.float64)
+            keep.append(md)
+            d.coef.modes = _ptr(md)
+            d.coef.n_modes = md.shape[-2]
+        if c.get("spheres") is not None:
+            sp = np.ascontiguousarray(c["spheres"], dtype=np.float64)
+            keep.append(sp)
+            d.coef.spheres = _ptr(sp)
+            d.coef.n_spheres = sp.shape[0]
+        d.f_value = float(problem.get("f_value", 1.0))
+        d.tol = float(tol)
+        d.maxit = int(maxit)
+        d.memory = memory
+        d.check_interval = int(check_interval)
+        if warm_basis is not None:
+            wb = np.ascontiguousarray(warm_basis, dtype=np.float64)
+            keep.append(wb)
+            d.warm_start = _abi.WARM_USER
+            d.warm_basis = _ptr(wb)
+        return d
+
+    @staticmethod
+    def basis_size(problem):
+        dim = problem["dim"]
+        nv = 1 << dim
+        if "n_fine_per_cell" in problem:
+            return int(np.sum(nv * (problem["n_fine_per_cell"].astype(np.int64) + 1) ** dim))
+        return problem["corners"].shape[0] * nv * (problem["n_fine"] + 1) ** dim
+
+    # -- calls --------------------------------------------------------------
+    def run(self, problem, precision="fp64", tol=1e-10, maxit=1000, want_basis=False,
+            warm_basis=None, check_interval=0, raise_on_failure=False):
+        keep = []
+        d = self.make_desc(problem, precision, tol, maxit, check_interval, warm_basis, keep=keep)
+        nc, nv = d.n_cells, 1 << d.dim
+        M = np.zeros((nc, nv, nv))
+        F = np.zeros((nc, nv))
+        status = np.zeros(nc, dtype=np.int32)
+        iters = np.zeros((nc, nv), dtype=np.int32)
+        basis = np.zeros(self.basis_size(problem)) if want_basis else None
+        st = _abi.Stats()
+        rc = self.lib.msfem_run_batch(self.handle, ctypes.byref(d), _ptr(M), _ptr(F), _ptr(basis),
+                                      _ptr(status), _ptr(iters), ctypes.byref(st))
+        if rc not in (_abi.OK, _abi.ERR_NOT_CONVERGED) or (raise_on_failure and rc != _abi.OK):
+            raise _abi.MsfemError(rc, _abi.last_error(self.lib))
+        return {"M": M, "F": F, "status": status, "iters": iters, "basis": basis,
+                "stats": st.as_dict(), "rc": rc}
+
+    def run_desc(self, desc, M, F, basis=None, status=None, iters=None, stats=True):
+        """Raw call with caller-owned pointers (ints or None), e.g. device buffers."""
+        st = _abi.Stats() if stats else None
+        rc = self.lib.msfem_run_batch(self.handle, ctypes.byref(desc), M, F, basis, status, iters,
+                                      ctypes.byref(st) if st is not None else None)
+        if rc not in (_abi.OK, _abi.ERR_NOT_CONVERGED):
+            raise _abi.MsfemError(rc, _abi.last_error(self.lib))
+        return rc, (st.as_dict() if st is not None else None)
+
+    def tabulate(self, problem, ncomp):
+        keep = []
+        d = self.make_desc(problem, keep=keep)
+        size = self.lib.msfem_tabulated_size(ctypes.byref(d), ncomp)
+        if size < 0:
+            raise _abi.MsfemError(_abi.ERR_INVALID_ARG, "cannot size the tabulation")
+        out = np.zeros(size)
+        rc = self.lib.msfem_tabulate_coefficient(self.handle, ctypes.byref(d), ncomp, _ptr(out))
+        if rc != _abi.OK:
+            raise _abi.MsfemError(rc, _abi.last_error(self.lib))
+        return out

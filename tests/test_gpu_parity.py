@@ -1,0 +1,170 @@
+"""GPU parity: the CUDA path through the C-ABI against the CPU FP64 oracle
+(banded Cholesky, exact to rounding) on the same seeded inputs.
+
+Tolerances: FP64 form solved to 1e-13 relative residual, compared at 1e-10
+relative (M, F) and 1e-9 absolute (basis values, which are O(1)); MIXED form
+(FP32 inner CG + FP64 refinement) at the same bars; iteration counts of the
+FP64 form equal the oracle's Jacobi-PCG restatement within +-2."""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL_REL = 1e-10
+
+
+def rel_err(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def check(got, ref, basis=True):
+    assert got["rc"] == 0, got["status"]
+    assert np.all(got["status"] == 0)
+    assert rel_err(got["M"], ref["M"]) < TOL_REL
+    assert rel_err(got["F"], ref["F"]) < TOL_REL
+    if basis:
+        assert np.abs(got["basis"] - ref["basis"]).max() < 1e-9
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_config1_parity(pkg, oracle, engine, precision):
+    prob = pkg.workloads.config1()
+    got = engine.run(prob, precision=precision, tol=1e-13, want_basis=True)
+    ref = oracle.run(prob, want_basis=True)
+    check(got, ref)
+    assert got["stats"]["max_rel_residual"] < 1e-12
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_reference_problem_parity(pkg, oracle, engine, precision):
+    """The reference's own MatrixCoeff (PI_D), f = 2, n_refine = 3, n_refine_local = 4."""
+    prob = pkg.workloads.reference_problem(2, 3, 4)
+    got = engine.run(prob, precision=precision, tol=1e-13, want_basis=True)
+    ref = oracle.run(prob, want_basis=True)
+    check(got, ref)
+
+
+def test_fp64_iterations_match_oracle_jacobi_pcg(pkg, oracle, engine):
+    prob = pkg.workloads.reference_problem(2, 2, 5)
+    got = engine.run(prob, precision="fp64", tol=1e-10, check_interval=1)
+    ref = oracle.run(prob, solver=oracle.SOLVER_JACOBI_CG, tol=1e-10)
+    assert np.abs(got["iters"] - ref["iters"]).max() <= 2
+    assert rel_err(got["M"], ref["M"]) < 1e-8
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_random_fourier_tensor_parity(pkg, oracle, engine, precision):
+    """Config-2 coefficient family on a subset of cells, N = 32, tabulated on the GPU."""
+    W = pkg.workloads
+    full = W.config2(K=64, N=32)
+    prob = W.subset(full, [0, 1, 63, 64, 2080, 4095])
+    got = engine.run(prob, precision=precision, tol=1e-13, want_basis=True)
+    # oracle evaluates the same Fourier field itself
+    ref = oracle.run(prob, want_basis=True)
+    check(got, ref)
+
+
+def test_tabulation_matches_oracle(pkg, oracle, engine):
+    W = pkg.workloads
+    prob = W.subset(W.config2(K=64, N=32), [5, 700])
+    a = engine.tabulate(prob, 3)
+    b = oracle.tabulate(prob, 3)
+    assert np.abs(a - b).max() < 1e-12 * np.abs(b).max()
+
+
+@pytest.mark.parametrize("geom", ["parallelogram", "bilinear"])
+def test_general_geometry(pkg, oracle, engine, geom):
+    W = pkg.workloads
+    c = W.unit_cube_corners(2, 4) * 0.8 + 0.05
+    if geom == "parallelogram":
+        c = c + c[:, :, 1:2] * np.array([0.2, 0.0])  # shear
+    else:
+        rng = np.random.default_rng(7)
+        c = c + rng.uniform(-0.01, 0.01, size=c.shape) * np.array([1, 1])
+    prob = W.problem(2, c, 12, {"kind": 1}, f_value=2.0)
+    got = engine.run(prob, precision="fp64", tol=1e-13, want_basis=True)
+    ref = oracle.run(prob, want_basis=True)
+    check(got, ref)
+
+
+def test_constant_tensor_known_answer(pkg, engine):
+    W = pkg.workloads
+    prob = W.problem(2, W.unit_cube_corners(2, 4), 16, {"kind": 0, "params": [3.0, 0.0, 0.5]})
+    got = engine.run(prob, precision="fp64", tol=1e-13)
+    H = 0.25
+    K1 = np.array([[1.0, -1.0], [-1.0, 1.0]]) / H
+    M1 = np.array([[2.0, 1.0], [1.0, 2.0]]) * H / 6.0
+    exact = 3.0 * np.kron(M1, K1) + 0.5 * np.kron(K1, M1)
+    assert np.abs(got["M"] - exact).max() < 1e-11
+    assert np.allclose(got["F"], H * H / 4, rtol=1e-12)
+
+
+@pytest.mark.parametrize("N", [1, 2, 3, 7, 16, 31, 32])
+def test_ragged_sizes(pkg, oracle, engine, N):
+    W = pkg.workloads
+    prob = W.problem(2, W.unit_cube_corners(2, 2), N, {"kind": 2, "params": [0.5, 0.25]})
+    got = engine.run(prob, precision="fp64", tol=1e-13, want_basis=True)
+    ref = oracle.run(prob, want_basis=True)
+    check(got, ref)
+
+
+def test_uneven_refinement_one_launch(pkg, oracle, engine):
+    W = pkg.workloads
+    corners = W.unit_cube_corners(2, 4)
+    nf = np.array([8, 16, 32, 24, 5, 32, 16, 8, 12, 32, 8, 16, 20, 4, 32, 9], dtype=np.int32)
+    prob = W.problem(2, corners, nf, {"kind": 1}, f_value=2.0)
+    for precision in ("fp64", "mixed"):
+        got = engine.run(prob, precision=precision, tol=1e-13, want_basis=True)
+        ref = oracle.run(prob, want_basis=True)
+        check(got, ref)
+        assert got["stats"]["kernel_launches"] == 1
+
+
+def test_warm_start_exact_basis_converges_immediately(pkg, oracle, engine):
+    prob = pkg.workloads.config1()
+    ref = oracle.run(prob, want_basis=True)
+    got = engine.run(prob, precision="fp64", tol=1e-10, want_basis=True, warm_basis=ref["basis"])
+    check(got, ref)
+    assert got["iters"].max() <= 1
+
+
+def test_maxit_reported_per_cell(pkg, engine):
+    prob = pkg.workloads.config1()
+    got = engine.run(prob, precision="fp64", tol=1e-13, maxit=3)
+    assert got["rc"] != 0
+    assert np.all(got["status"] == pkg._abi.CELL_MAXIT)
+
+
+def test_nan_coefficient_reported(pkg, engine, oracle):
+    W = pkg.workloads
+    prob = W.problem(2, W.unit_cube_corners(2, 2), 8, {"kind": 2, "params": [0.5, 0.25]})
+    tab = oracle.tabulate(prob, 1)
+    nfc = 64
+    tab[1 * 4 * nfc + 17] = np.nan  # cell 1, q 0, fine cell 17
+    tprob = dict(prob)
+    tprob["coef"] = {"kind": 5, "ncomp": 1, "qp_values": tab}
+    got = engine.run(tprob, precision="fp64", tol=1e-12)
+    assert got["status"][1] == pkg._abi.CELL_NAN
+    assert np.all(got["status"][[0, 2, 3]] == 0)
+
+
+def test_degenerate_cell_reported(pkg, engine):
+    W = pkg.workloads
+    c = W.unit_cube_corners(2, 2).copy()
+    c[2] = c[2][0]  # all four corners equal
+    prob = W.problem(2, c, 8, {"kind": 0, "params": [1, 0, 1]})
+    got = engine.run(prob, precision="fp64", tol=1e-12)
+    assert got["status"][2] == pkg._abi.CELL_BAD_INPUT
+    assert np.all(got["status"][[0, 1, 3]] == 0)
+
+
+def test_mixed_reaches_tolerance_and_matches_fp64(pkg, engine):
+    W = pkg.workloads
+    prob = W.subset(W.config2(K=64, N=32), list(range(0, 4096, 97)))
+    a = engine.run(prob, precision="fp64", tol=1e-10)
+    b = engine.run(prob, precision="mixed", tol=1e-10)
+    assert a["stats"]["max_rel_residual"] < 1e-10
+    assert b["stats"]["max_rel_residual"] < 1e-10
+    assert rel_err(b["M"], a["M"]) < 1e-9
