@@ -1,0 +1,416 @@
+#!/usr/bin/env python
+"""Benchmark: MsFEM basis solves/s on one GB300 (per rank), one JSON line.
+
+Workload (one step = one pass of the hot path over the batch):
+  2D unit square, 64x64 coarse Q1 cells (4096), 32x32 fine Q1 cells per
+  coarse cell (1089 nodes), 4 Dirichlet basis solves per cell (16384 solves),
+  random-Fourier SPD tensor A = R(theta) diag(e^g1, e^g2) R(theta)^T (64
+  modes per field, |k| <= 128 pi, amplitudes N(0, 1/64), seeds 2/20/200),
+  f = 1, CG to 1e-10 relative residual.  Synthetic, seeded; the coefficient is
+  tabulated at the QGauss(2) points once (input data, 403 MB, larger than L2)
+  and stays resident in HBM.
+
+value      device-resident FP64 form (the drop-in), CUDA events on the
+           launching stream, max over ranks.
+mixed      same workload, FP32 inner CG + FP64 refinement.
+e2e        the public C-ABI call with pinned HOST buffers: H2D of the corners
+           and the tabulated field, D2H of M and F, every step.
+roofline   FP64 FMA pipe (the kernel is bound by it; HBM fraction reported too).
+cpu_baseline  the oracle's restatement of the reference algorithm (SSOR(1.6)
+           preconditioned CG on CSR, QGauss(2) assembly, 2^d x 2^d SpMV
+           epilogue) on a bounded sample of the same workload, all host cores.
+
+--impl reference  the reference algorithm on the host cores only (the
+           reference itself cannot be built: deal.II/p4est/Trilinos/MPI absent).
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+import __graft_entry__ as graft  # noqa: E402
+
+METRIC = "MsFEM basis solves/s at 1e-10 rel residual, plain FP64 vs mixed+surrogate, 1 GB300"
+UNIT = "basis solves/s"
+TOL = 1e-10
+K_COARSE, N_FINE = 64, 32
+WORKLOAD = ("2D MsFEM local basis: 64x64 coarse Q1 cells, 32x32 fine Q1 per cell, 4 RHS per cell, "
+            "random-Fourier SPD tensor (seeds 2/20/200), f=1, CG to 1e-10 rel residual")
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def flops_per_solve_iter(N):
+    """SURVEY-style algorithmic work of one CG iteration of one solve (2D):
+    2 nnz(A_II) + 11 n_I, nnz(A_II) = (3N-5)^2, n_I = (N-1)^2."""
+    return 2 * (3 * N - 5) ** 2 + 11 * (N - 1) ** 2
+
+
+def flops_one_off_per_cell(N):
+    """Epilogue 2^d 2 nnz + (2^2d + 2^d) 2 n^d, assembly N^d 2^d (2^2d (2d+1))."""
+    n = N + 1
+    return 4 * 2 * (3 * n - 2) ** 2 + (16 + 4) * 2 * n * n + N * N * 4 * (16 * 5)
+
+
+def load_probe(pkg):
+    lib = ctypes.CDLL(os.path.join(pkg.build.LIB_DIR, "libmsfem_probe.so"))
+    lib.msfem_probe_fma_flops.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    lib.msfem_probe_fma_flops.restype = ctypes.c_int
+    return lib
+
+
+def read_peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def read_profile_traffic(name):
+    """dram bytes per launch recorded from an ncu capture (profiles/*.txt)."""
+    path = os.path.join(REPO, "profiles", name)
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100", "-i", str(device)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        mhz, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                mhz.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not mhz:
+            return None
+        busy = [m for m in mhz if mx and m > 0.5 * mx] or mhz
+        return {"sm_mhz": statistics.median(busy), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(mhz)}
+
+
+def cpu_reference(pkg, oracle, prob_cells, nthreads, steps=1, warmup=0):
+    """The reference algorithm (SSOR(1.6)-PCG, CSR, QGauss(2) assembly) on a
+    sample of cells; the tabulated coefficient is prepared untimed."""
+    tab = oracle.tabulate(prob_cells, 3)
+    tprob = dict(prob_cells)
+    tprob["coef"] = {"kind": pkg._abi.COEF_TABULATED, "ncomp": 3, "qp_values": tab}
+    times = []
+    res = None
+    for it in range(warmup + steps):
+        t0 = time.perf_counter()
+        res = oracle.run(tprob, solver=oracle.SOLVER_SSOR_CG, tol=TOL, tol_absolute=False,
+                         maxit=1000, omega=1.6, ordering=oracle.ORDER_DEALII, nthreads=nthreads)
+        dt = time.perf_counter() - t0
+        if it >= warmup:
+            times.append(dt)
+    solves = prob_cells["corners"].shape[0] * 4
+    return solves, times, res
+
+
+def run_reference_arm(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    pkg = graft.load_package()
+    oracle = graft.load_oracle()
+    oracle.build()
+    W = pkg.workloads
+    full = W.config2(K=K_COARSE, N=N_FINE)
+    nthreads = os.cpu_count() or 1
+    n_sample = max(16, min(4096, 64 * nthreads))
+    cells = np.linspace(0, K_COARSE * K_COARSE - 1, n_sample).astype(int)
+    sample = W.subset(full, cells)
+    solves, times, res = cpu_reference(pkg, oracle, sample, nthreads, steps=args.steps,
+                                       warmup=args.warmup)
+    t = sum(times) / len(times)
+    value = solves / t
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded random-Fourier coefficient)",
+        "config": {"workload": WORKLOAD, "precision": "fp64", "sample_cells": int(n_sample)},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                         "sample": f"{n_sample} of 4096 coarse cells per step ({solves} solves), "
+                                   "SSOR(1.6)-PCG to 1e-10 rel, deal.II dof order"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "mean_iterations": float(res["iters"].mean()),
+        "note": ("reference cannot be built here (deal.II/p4est/Trilinos/MPI absent); this is "
+                 "the oracle's restatement of its local-basis algorithm"),
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        run_reference_arm(args)
+        return
+
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    pkg = graft.load_package()
+    pkg.build.build_all()
+    abi = pkg._abi
+    W = pkg.workloads
+    eng = pkg.Engine(local)
+    stream = torch.cuda.current_stream()
+    eng.set_stream(stream.cuda_stream)
+
+    # ---- workload on the device: corners + tabulated coefficient (weak scaling:
+    # every rank owns its own 64x64 block of coarse cells)
+    prob = W.config2(K=K_COARSE, N=N_FINE)
+    corners_h = prob["corners"] + np.array([float(rank), 0.0])
+    n_cells = corners_h.shape[0]
+    solves_rank = 4 * n_cells
+    corners_d = torch.from_numpy(np.ascontiguousarray(corners_h)).to(f"cuda:{local}")
+    modes = np.ascontiguousarray(prob["coef"]["modes"])
+    dtab = abi.BatchDesc()
+    dtab.dim, dtab.n_cells, dtab.n_fine = 2, n_cells, N_FINE
+    dtab.corners = corners_d.data_ptr()
+    dtab.coef.kind = abi.COEF_FOURIER
+    dtab.coef.modes = modes.ctypes.data  # mode table: host memory is accepted for tabulation input
+    dtab.coef.n_modes = modes.shape[1]
+    dtab.memory = abi.MEM_HOST
+    dtab.tol, dtab.maxit = TOL, 1000
+    size = eng.lib.msfem_tabulated_size(ctypes.byref(dtab), 3)
+    tab_d = torch.empty(size, dtype=torch.float64, device=f"cuda:{local}")
+    # tabulate on the host-memory path into a host buffer is slow for 400 MB; use
+    # the device path: device corners + device mode table
+    modes_d = torch.from_numpy(modes).to(f"cuda:{local}")
+    dtab.coef.modes = modes_d.data_ptr()
+    dtab.memory = abi.MEM_DEVICE
+    rc = eng.lib.msfem_tabulate_coefficient(eng.handle, ctypes.byref(dtab), 3, tab_d.data_ptr())
+    if rc != abi.OK:
+        raise abi.MsfemError(rc, abi.last_error(eng.lib))
+
+    def device_desc(precision):
+        d = abi.BatchDesc()
+        d.dim, d.n_cells, d.n_fine = 2, n_cells, N_FINE
+        d.precision = precision
+        d.corners = corners_d.data_ptr()
+        d.coef.kind = abi.COEF_TABULATED
+        d.coef.ncomp = 3
+        d.coef.qp_values = tab_d.data_ptr()
+        d.f_value = 1.0
+        d.tol, d.maxit = TOL, 1000
+        d.memory = abi.MEM_DEVICE
+        return d
+
+    M_d = torch.empty((n_cells, 4, 4), dtype=torch.float64, device=f"cuda:{local}")
+    F_d = torch.empty((n_cells, 4), dtype=torch.float64, device=f"cuda:{local}")
+    st_d = torch.empty(n_cells, dtype=torch.int32, device=f"cuda:{local}")
+    it_d = torch.empty((n_cells, 4), dtype=torch.int32, device=f"cuda:{local}")
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    def max_over_ranks(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{local}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    def timed(precision, steps, warmup, sample_clocks=False):
+        d = device_desc(precision)
+        args_ = (M_d.data_ptr(), F_d.data_ptr(), None, st_d.data_ptr(), it_d.data_ptr())
+        for _ in range(warmup):
+            eng.run_desc(d, *args_, stats=False)
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        sampler = ClockSampler(local) if sample_clocks else None
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            eng.run_desc(d, *args_, stats=False)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        clocks = sampler.stop() if sampler else None
+        barrier()
+        ms = e0.elapsed_time(e1) / steps
+        # correctness / work accounting of the same workload (untimed)
+        _, st = eng.run_desc(d, *args_, stats=True)
+        return max_over_ranks(ms), st, clocks
+
+    # ---- FP64 form (headline)
+    ms64, st64, clocks = timed(abi.PREC_FP64, args.steps, args.warmup, sample_clocks=True)
+    value = world * solves_rank / (ms64 * 1e-3)
+    probe = load_probe(pkg)
+    fp64_peak = ctypes.c_double(0.0)
+    fp32_peak = ctypes.c_double(0.0)
+    probe.msfem_probe_fma_flops(1, ctypes.byref(fp64_peak))
+    probe.msfem_probe_fma_flops(0, ctypes.byref(fp32_peak))
+    flops64 = (st64["iterations_total"] * flops_per_solve_iter(N_FINE)
+               + n_cells * flops_one_off_per_cell(N_FINE))
+    achieved = flops64 / (ms64 * 1e-3) / 1e12
+    peaks, peak_src = read_peaks()
+    alg_bytes = size * 8 + n_cells * (8 * 2 * 4 + 8 * 20 + 4 * 5)  # field + corners + outputs
+    traffic = read_profile_traffic("msfem2d_fp64_config2.txt")
+    roofline = {
+        "bound": "fp64", "achieved": achieved, "peak": fp64_peak.value / 1e12, "unit": "TFLOP/s",
+        "frac": achieved / (fp64_peak.value / 1e12),
+        "traffic": traffic,
+        "peak_source": "measured in this run: FP64 FMA probe (libmsfem_probe.so), 8 independent "
+                       "FMA chains per thread, 8 CTAs x 256 threads per SM",
+        "kernel": "msfem2d_kernel<32,256,FP64>",
+        "flops_per_launch": flops64,
+        "algorithmic_bytes_per_launch": alg_bytes,
+        "hbm": {"achieved": alg_bytes / (ms64 * 1e-3) / 1e9, "peak": peaks.get("hbm_gbs"),
+                "unit": "GB/s", "frac": alg_bytes / (ms64 * 1e-3) / 1e9 / peaks.get("hbm_gbs", 1),
+                "peak_source": peak_src},
+    }
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms64, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded random-Fourier SPD coefficient, tabulated at Gauss points)",
+        "config": {"workload": WORKLOAD, "precision": "fp64", "coarse_cells_per_gpu": n_cells,
+                   "fine_cells_per_coarse": N_FINE * N_FINE, "rhs_per_cell": 4,
+                   "solves_per_step_per_gpu": solves_rank, "tol": TOL,
+                   "l2": "inputs larger than L2 (403 MB tabulated field per step)",
+                   "parallelism": f"replicas: {world} GPU(s), cells sharded, no collective"},
+        "roofline": roofline,
+        "gpu_launches": args.steps * st64["kernel_launches"],
+        "clocks": clocks,
+        "stats": {"mean_iterations": st64["iterations_total"] / max(1, st64["solves"]),
+                  "max_iterations": st64["iterations_max"],
+                  "max_rel_residual": st64["max_rel_residual"],
+                  "cells_failed": st64["cells_failed"], "ctas_per_sm": st64["ctas_per_sm"]},
+    }
+    # ---- mixed form
+    if not args.no_mixed:
+        msmx, stmx, _ = timed(abi.PREC_MIXED, args.steps, args.warmup)
+        line["mixed"] = {
+            "value": world * solves_rank / (msmx * 1e-3), "ms_per_step": msmx,
+            "speedup_vs_fp64": ms64 / msmx,
+            "mean_inner_iterations": stmx["iterations_total"] / max(1, stmx["solves"]),
+            "max_refinements": stmx["refinements_max"],
+            "max_rel_residual": stmx["max_rel_residual"], "cells_failed": stmx["cells_failed"],
+            "fp32_peak_tflops": fp32_peak.value / 1e12,
+        }
+    # ---- e2e through the public C-ABI with pinned host buffers
+    if not args.no_e2e:
+        tab_h = torch.empty(size, dtype=torch.float64, pin_memory=True)
+        tab_h.copy_(tab_d.cpu())
+        corners_pin = torch.from_numpy(np.ascontiguousarray(corners_h)).pin_memory()
+        M_h = torch.empty((n_cells, 4, 4), dtype=torch.float64, pin_memory=True)
+        F_h = torch.empty((n_cells, 4), dtype=torch.float64, pin_memory=True)
+        st_h = torch.empty(n_cells, dtype=torch.int32, pin_memory=True)
+        d = device_desc(abi.PREC_FP64)
+        d.memory = abi.MEM_HOST
+        d.corners = corners_pin.data_ptr()
+        d.coef.qp_values = tab_h.data_ptr()
+        for _ in range(2):
+            eng.run_desc(d, M_h.data_ptr(), F_h.data_ptr(), None, st_h.data_ptr(), None, stats=False)
+        torch.cuda.synchronize()
+        barrier()
+        e_steps = max(3, args.steps // 2)
+        t0 = time.perf_counter()
+        for _ in range(e_steps):
+            eng.run_desc(d, M_h.data_ptr(), F_h.data_ptr(), None, st_h.data_ptr(), None, stats=False)
+        torch.cuda.synchronize()
+        e2e_s = max_over_ranks((time.perf_counter() - t0) / e_steps)
+        line["e2e"] = {"value": world * solves_rank / e2e_s, "unit": UNIT,
+                       "ms_per_step": e2e_s * 1e3,
+                       "h2d_bytes_per_step": int(size * 8 + corners_h.nbytes),
+                       "d2h_bytes_per_step": int(M_h.numel() * 8 + F_h.numel() * 8 + st_h.numel() * 4)}
+        # sanity: host result equals the device-resident one
+        line["e2e"]["matches_device"] = bool(np.array_equal(M_h.numpy(), M_d.cpu().numpy()))
+    # ---- CPU baseline (rank 0, N = 1 only)
+    if rank == 0 and world == 1 and not args.no_cpu:
+        oracle = graft.load_oracle()
+        oracle.build()
+        nthreads = os.cpu_count() or 1
+        n_sample = max(16, min(2048, 128 * nthreads))
+        cells = np.linspace(0, n_cells - 1, n_sample).astype(int)
+        sample = W.subset(prob, cells)
+        solves, times, res = cpu_reference(pkg, oracle, sample, nthreads, steps=1, warmup=0)
+        cv = solves / times[0]
+        line["cpu_baseline"] = {
+            "value": cv, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": f"{n_sample} of {n_cells} coarse cells ({solves} solves), SSOR(1.6)-PCG to "
+                      "1e-10 rel, CSR, QGauss(2) assembly, 16-SpMV epilogue",
+            "seconds": times[0], "mean_iterations": float(res["iters"].mean())}
+        # parity of the sampled cells against the GPU result
+        got_M = M_d.cpu().numpy()[cells]
+        line["cpu_baseline"]["max_rel_diff_M_vs_gpu"] = float(
+            np.abs(got_M - res["M"]).max() / np.abs(res["M"]).max())
+    if rank == 0:
+        print(json.dumps(line))
+    eng.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -55,10 +55,23 @@ def _sources(folder, exts):
 def build_gpu(force=False, quiet=True, extra=()):
     os.makedirs(LIB_DIR, exist_ok=True)
     target = os.path.join(LIB_DIR, "libmsfem_gpu.so")
-    deps = _sources(CSRC, (".cu", ".cuh", ".h")) + [os.path.join(INCLUDE, "msfem_gpu.h")]
+    deps = [f for f in _sources(CSRC, (".cu", ".cuh", ".h")) if not f.endswith("probe.cu")]
+    deps += [os.path.join(INCLUDE, "msfem_gpu.h")]
     if force or _stale(target, deps):
         cmd = [_nvcc(), *ARCH, *NVCC_FLAGS, *extra, "-I", INCLUDE, "-I", CSRC,
                "-o", target + ".tmp", os.path.join(CSRC, "msfem_gpu.cu")]
+        _run(cmd, quiet)
+        os.replace(target + ".tmp", target)
+    return target
+
+
+def build_probe(force=False, quiet=True):
+    """FMA-rate probe used by bench.py for the roofline denominator."""
+    os.makedirs(LIB_DIR, exist_ok=True)
+    target = os.path.join(LIB_DIR, "libmsfem_probe.so")
+    src = os.path.join(CSRC, "probe.cu")
+    if force or _stale(target, [src]):
+        cmd = [_nvcc(), *ARCH, *NVCC_FLAGS, "-o", target + ".tmp", src]
         _run(cmd, quiet)
         os.replace(target + ".tmp", target)
     return target
@@ -83,4 +96,4 @@ def build_host(force=False, quiet=True):
 
 
 def build_all(force=False, quiet=True):
-    return [build_gpu(force, quiet), build_host(force, quiet)]
+    return [build_gpu(force, quiet), build_probe(force, quiet), build_host(force, quiet)]

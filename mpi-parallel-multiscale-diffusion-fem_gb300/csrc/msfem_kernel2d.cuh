@@ -34,16 +34,19 @@ template <int NMAX>
 struct Smem2D {
   static constexpr int P = NMAX + 3;
   static constexpr int G = P * P;
+  // every array starts on a 128-byte boundary (vector loads need 16 B)
+  static constexpr size_t al(size_t x) { return (x + 127) & ~size_t(127); }
   static constexpr size_t kC64 = 0;
-  static constexpr size_t kV64 = kC64 + sizeof(double) * 4 * G;
-  static constexpr size_t kS64 = kV64 + sizeof(double) * 4 * G;
-  static constexpr size_t kD64 = kS64 + sizeof(double) * G;
-  static constexpr size_t kB64 = kD64 + sizeof(double) * G;
-  static constexpr size_t kEndFP64 = kB64 + sizeof(double) * G;
+  static constexpr size_t kV64 = al(kC64 + sizeof(double) * 4 * G);
+  static constexpr size_t kS64 = al(kV64 + sizeof(double) * 4 * G);
+  static constexpr size_t kD64 = al(kS64 + sizeof(double) * G);
+  static constexpr size_t kB64 = al(kD64 + sizeof(double) * G);
+  static constexpr size_t kEndFP64 = al(kB64 + sizeof(double) * G);
   static constexpr size_t kC32 = kEndFP64;
-  static constexpr size_t kV32 = kC32 + sizeof(float) * 4 * G;
-  static constexpr size_t kEndMixed = kV32 + sizeof(float) * 4 * G;
+  static constexpr size_t kV32 = al(kC32 + sizeof(float) * 4 * G);
+  static constexpr size_t kEndMixed = al(kV32 + sizeof(float) * 4 * G);
   static constexpr size_t bytes(bool mixed) { return mixed ? kEndMixed : kEndFP64; }
+  static_assert(kV64 % 16 == 0 && kC32 % 16 == 0 && kV32 % 16 == 0, "vector alignment");
 };
 
 __device__ __forceinline__ void ld4(const double *__restrict__ v, int g, double (&t)[4]) {
@@ -548,11 +551,17 @@ msfem2d_kernel(const KernelParams p) {
           if (lane < 4) {
             double a = 0.0;
             if (cs.active[lane]) {
-              a = cs.rho[lane] / t;
-              if (!isfinite(a) || !(t > 0.0)) {
-                a = 0.0;
+              if (cs.rho[lane] == 0.0) {
+                // exact solution reached in the previous step
                 cs.active[lane] = 0;
-                cs.iters[lane] = -it;  // breakdown marker
+                cs.iters[lane] = it - 1;
+              } else {
+                a = cs.rho[lane] / t;
+                if (!isfinite(a) || !(t > 0.0)) {
+                  a = 0.0;
+                  cs.active[lane] = 0;
+                  cs.iters[lane] = -it;  // breakdown marker
+                }
               }
             }
             cs.alpha[lane] = a;
@@ -601,7 +610,7 @@ msfem2d_kernel(const KernelParams p) {
               if (!isfinite(t)) {
                 cs.active[lane] = 0;
                 cs.iters[lane] = -it;
-              } else if (need_nu && nu <= tol2 * cs.bb[lane]) {
+              } else if (t == 0.0 || (need_nu && nu <= tol2 * cs.bb[lane])) {
                 cs.active[lane] = 0;
                 cs.iters[lane] = it;
               } else if (it >= p.maxit) {
@@ -657,7 +666,6 @@ msfem2d_kernel(const KernelParams p) {
         double t[4] = {gv[0] * sq, gv[1] * sq, gv[2] * sq, gv[3] * sq};
         st4(v64, g, t);
       }
-      if (tid < 4) total_iters[0] = 0;
       __syncthreads();
       if (tid == 0) cs.refinements = 0;
     } else {
@@ -896,7 +904,7 @@ msfem2d_kernel(const KernelParams p) {
           }
         }
         if (lane == 0) {
-          int st = MSFEM_CELL_CONVERGED;
+          int st = cs.status;  // MSFEM_CELL_NAN when a diagonal was not positive
           for (int r = 0; r < 4; ++r) {
             const int itv = cs.iters[r];
             if (itv <= -1000000) st = st == MSFEM_CELL_CONVERGED ? MSFEM_CELL_MAXIT : st;
