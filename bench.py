@@ -202,6 +202,8 @@ def main():
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 timing (profiling runs)")
+    ap.add_argument("--coarse", type=int, default=K_COARSE, help="coarse cells per direction")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -220,12 +222,15 @@ def main():
     abi = pkg._abi
     W = pkg.workloads
     eng = pkg.Engine(local)
-    stream = torch.cuda.current_stream()
+    # a dedicated (non-default) stream, current for torch and used by the
+    # library, so the CUDA events below bracket the kernels themselves
+    stream = torch.cuda.Stream(device=local)
+    torch.cuda.set_stream(stream)
     eng.set_stream(stream.cuda_stream)
 
     # ---- workload on the device: corners + tabulated coefficient (weak scaling:
     # every rank owns its own 64x64 block of coarse cells)
-    prob = W.config2(K=K_COARSE, N=N_FINE)
+    prob = W.config2(K=args.coarse, N=N_FINE)
     corners_h = prob["corners"] + np.array([float(rank), 0.0])
     n_cells = corners_h.shape[0]
     solves_rank = 4 * n_cells
@@ -303,6 +308,10 @@ def main():
         return max_over_ranks(ms), st, clocks
 
     # ---- FP64 form (headline)
+    if args.no_fp64:
+        msmx, stmx, _ = timed(abi.PREC_MIXED, args.steps, args.warmup)
+        print(json.dumps({"profile_only": "mixed", "ms_per_step": msmx}))
+        return
     ms64, st64, clocks = timed(abi.PREC_FP64, args.steps, args.warmup, sample_clocks=True)
     value = world * solves_rank / (ms64 * 1e-3)
     probe = load_probe(pkg)
@@ -334,7 +343,9 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms64, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded random-Fourier SPD coefficient, tabulated at Gauss points)",
-        "config": {"workload": WORKLOAD, "precision": "fp64", "coarse_cells_per_gpu": n_cells,
+        "config": {"workload": WORKLOAD if args.coarse == K_COARSE else
+                   WORKLOAD.replace("64x64", f"{args.coarse}x{args.coarse}"),
+                   "precision": "fp64", "coarse_cells_per_gpu": n_cells,
                    "fine_cells_per_coarse": N_FINE * N_FINE, "rhs_per_cell": 4,
                    "solves_per_step_per_gpu": solves_rank, "tol": TOL,
                    "l2": "inputs larger than L2 (403 MB tabulated field per step)",
@@ -347,6 +358,7 @@ def main():
                   "max_rel_residual": st64["max_rel_residual"],
                   "cells_failed": st64["cells_failed"], "ctas_per_sm": st64["ctas_per_sm"]},
     }
+    M64 = M_d.cpu().numpy().copy()
     # ---- mixed form
     if not args.no_mixed:
         msmx, stmx, _ = timed(abi.PREC_MIXED, args.steps, args.warmup)
@@ -385,7 +397,7 @@ def main():
                        "h2d_bytes_per_step": int(size * 8 + corners_h.nbytes),
                        "d2h_bytes_per_step": int(M_h.numel() * 8 + F_h.numel() * 8 + st_h.numel() * 4)}
         # sanity: host result equals the device-resident one
-        line["e2e"]["matches_device"] = bool(np.array_equal(M_h.numpy(), M_d.cpu().numpy()))
+        line["e2e"]["matches_device"] = bool(np.array_equal(M_h.numpy(), M64))
     # ---- CPU baseline (rank 0, N = 1 only)
     if rank == 0 and world == 1 and not args.no_cpu:
         oracle = graft.load_oracle()
@@ -402,7 +414,7 @@ def main():
                       "1e-10 rel, CSR, QGauss(2) assembly, 16-SpMV epilogue",
             "seconds": times[0], "mean_iterations": float(res["iters"].mean())}
         # parity of the sampled cells against the GPU result
-        got_M = M_d.cpu().numpy()[cells]
+        got_M = M64[cells]
         line["cpu_baseline"]["max_rel_diff_M_vs_gpu"] = float(
             np.abs(got_M - res["M"]).max() / np.abs(res["M"]).max())
     if rank == 0:

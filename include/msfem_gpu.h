@@ -180,7 +180,8 @@ int msfem_create(msfem_handle **handle, int device);
 int msfem_destroy(msfem_handle *handle);
 
 /* Launch on this stream (a cudaStream_t) instead of the handle's own.  NULL
- * restores the handle's stream. */
+ * restores the handle's own stream; to launch on the legacy default stream
+ * pass cudaStreamLegacy. */
 int msfem_set_stream(msfem_handle *handle, void *cuda_stream);
 
 /* Compute the multiscale basis of a batch of coarse cells.
