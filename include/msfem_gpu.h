@@ -209,6 +209,42 @@ int msfem_tabulate_coefficient(msfem_handle *handle,
 /* Number of doubles msfem_tabulate_coefficient writes for this batch. */
 int64_t msfem_tabulated_size(const msfem_batch_desc *desc, int32_t ncomp);
 
+/* Largest batch msfem_run_batch_noalloc accepts (its fixed scratch holds a
+ * work-queue counter plus 12 bytes per cell: about 0.75 MB per device). */
+#define MSFEM_NOALLOC_MAX_CELLS 65536
+
+/* No counterpart in the reference: an entry point for callers that cannot
+ * allocate device memory.  cudaMalloc synchronises the whole device and is
+ * illegal while a stream is being captured, so a caller running inside its own
+ * captured graph, inside a latency-critical time loop, or under a framework
+ * that owns every device allocation (a fixed memory budget or pool) cannot use
+ * msfem_run_batch, whose first call sizes device buffers on demand.
+ *
+ * This variant of the 2D basis kernel allocates nothing: no cudaMalloc, no
+ * cudaFree, no handle, no allocating library call.  Its scratch (the
+ * work-queue counter and per-cell residual / refinement words) is one
+ * file-scope device array of fixed size in libmsfem_gpu.so, which every GPU
+ * that loads the library holds until the process exits.
+ *   - 2D only, uniform N (n_fine_per_cell must be NULL), desc->memory must be
+ *     MSFEM_MEM_DEVICE: every pointer in desc and every output is a device
+ *     pointer the caller owns.  Coefficient kinds CONSTANT, REFERENCE, SINSIN
+ *     and TABULATED (FOURIER/SPHERES need a tabulation buffer: tabulate first).
+ *   - n_cells above MSFEM_NOALLOC_MAX_CELLS is rejected (MSFEM_ERR_INVALID_ARG).
+ *   - The first call on a device looks up the scratch array's device address
+ *     (with that device current); make that first call before any stream
+ *     capture begins.
+ *   - The call only enqueues work on `stream` (a cudaStream_t, NULL = legacy
+ *     default stream) and returns; outputs are valid once the stream has
+ *     completed, and per-cell failures are reported in cell_status only.
+ *   - All calls share the one scratch array, which keeps the last call's
+ *     contents; the counter is cleared on `stream` before each launch.  Calls
+ *     that may overlap on the GPU (different streams without ordering) race on
+ *     it: serialise them.
+ * Results equal msfem_run_batch's on the same inputs. */
+int msfem_run_batch_noalloc(const msfem_batch_desc *desc, double *M, double *F,
+                            double *basis, int32_t *cell_status,
+                            int32_t *iterations, void *stream);
+
 /* Message of the last failing call on this thread. */
 int msfem_last_error(char *buf, size_t len);
 

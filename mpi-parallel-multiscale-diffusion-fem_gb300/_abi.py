@@ -43,6 +43,7 @@ WARM_USER = 1
 
 MAX_N_2D = 32
 MAX_N_3D = 24
+NOALLOC_MAX_CELLS = 65536
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _i32p = ctypes.POINTER(ctypes.c_int32)
@@ -115,6 +116,9 @@ EXPORTS = {
     "msfem_tabulate_coefficient": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BatchDesc),
                                                   ctypes.c_int32, ctypes.c_void_p]),
     "msfem_tabulated_size": (ctypes.c_int64, [ctypes.POINTER(BatchDesc), ctypes.c_int32]),
+    "msfem_run_batch_noalloc": (ctypes.c_int, [ctypes.POINTER(BatchDesc), ctypes.c_void_p,
+                                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                               ctypes.c_void_p, ctypes.c_void_p]),
     "msfem_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
     "msfem_version": (ctypes.c_char_p, []),
 }

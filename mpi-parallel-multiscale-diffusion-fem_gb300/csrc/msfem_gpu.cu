@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -447,7 +448,118 @@ int run_tabulate(msfem_handle *h, const msfem_batch_desc *d, const std::vector<i
 
 }  // namespace
 
+// ---------------------------------------------------------------------------
+// Scratch of msfem_run_batch_noalloc: one fixed device array per GPU that
+// loads this library (held until the process exits).  Layout: work-queue
+// counter in the first 256 bytes, then rel_res [MAX] doubles, then
+// refinements [MAX] int32.  Device code could name it directly; host code
+// must fetch its device address with cudaGetSymbolAddress (the host-side name
+// is only a stand-in for the device object).
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kNoallocRelres = 256;
+constexpr size_t kNoallocRefine = kNoallocRelres + sizeof(double) * MSFEM_NOALLOC_MAX_CELLS;
+constexpr size_t kNoallocBytes = kNoallocRefine + sizeof(int32_t) * MSFEM_NOALLOC_MAX_CELLS;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[kMaxDevices] = {};
+
+// Once per device, with that device current: the scratch array's address.
+int noalloc_scratch(int device, void **out) {
+  if (device < 0 || device >= kMaxDevices) return fail(MSFEM_ERR_INVALID_ARG, "device id out of range");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[device]) {
+    void *ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess || !ptr)
+      return fail(MSFEM_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+    g_noalloc_ptr[device] = ptr;
+  }
+  *out = g_noalloc_ptr[device];
+  return MSFEM_OK;
+}
+
+}  // namespace
+
 extern "C" {
+
+int msfem_run_batch_noalloc(const msfem_batch_desc *d, double *M, double *F, double *basis,
+                            int32_t *cell_status, int32_t *iterations, void *stream) {
+  int rc = validate(d);
+  if (rc) return rc;
+  if (d->dim != 2) return fail(MSFEM_ERR_UNSUPPORTED, "msfem_run_batch_noalloc: 2D only");
+  if (d->memory != MSFEM_MEM_DEVICE)
+    return fail(MSFEM_ERR_INVALID_ARG, "msfem_run_batch_noalloc: desc->memory must be MSFEM_MEM_DEVICE");
+  if (d->n_fine_per_cell)
+    return fail(MSFEM_ERR_INVALID_ARG, "msfem_run_batch_noalloc: uniform N only (n_fine_per_cell must be NULL)");
+  if (d->n_cells > MSFEM_NOALLOC_MAX_CELLS)
+    return fail(MSFEM_ERR_INVALID_ARG, "msfem_run_batch_noalloc: n_cells " + std::to_string(d->n_cells) +
+                                           " exceeds MSFEM_NOALLOC_MAX_CELLS (" +
+                                           std::to_string(MSFEM_NOALLOC_MAX_CELLS) + ")");
+  const int kind = d->coef.kind;
+  if (kind != MSFEM_COEF_CONSTANT && kind != MSFEM_COEF_REFERENCE && kind != MSFEM_COEF_SINSIN &&
+      kind != MSFEM_COEF_TABULATED)
+    return fail(MSFEM_ERR_UNSUPPORTED, "msfem_run_batch_noalloc: tabulate FOURIER/SPHERES coefficients first");
+  if (d->n_cells > 0 && (!M || !F || !cell_status))
+    return fail(MSFEM_ERR_INVALID_ARG, "msfem_run_batch_noalloc: M, F and cell_status are required");
+  if (d->n_cells == 0) return MSFEM_OK;
+  const bool mixed = d->precision == MSFEM_PREC_MIXED;
+  Launch L{};
+  if (pick2d(d->n_fine, mixed, &L) != 0) return fail(MSFEM_ERR_UNSUPPORTED, "no kernel for this N");
+  int device = 0;
+  MSFEM_CUDA(cudaGetDevice(&device));
+  void *scratch = nullptr;
+  if ((rc = noalloc_scratch(device, &scratch))) return rc;
+  unsigned char *base = static_cast<unsigned char *>(scratch);
+
+  KernelParams p{};
+  p.dim = 2;
+  p.n_cells = d->n_cells;
+  p.n_fine_uniform = d->n_fine;
+  p.corners = d->corners;
+  p.n_fine = nullptr;
+  p.order = nullptr;
+  p.queue = reinterpret_cast<unsigned int *>(base);
+  p.coef_kind = kind;
+  p.ncomp = d->coef.ncomp;
+  for (int k = 0; k < 8; ++k) p.cparams[k] = d->coef.params[k];
+  if (kind == MSFEM_COEF_REFERENCE) reference_rrt(2, p.cparams);
+  p.qp_values = d->coef.qp_values;
+  p.qp_offset = d->coef.qp_offset;
+  p.f_value = d->f_value;
+  p.tol = d->tol;
+  p.maxit = d->maxit;
+  p.check_interval = d->check_interval;
+  p.inner_tol = 1e-4f;
+  p.inner_maxit = std::max(1, std::min(d->maxit, 1000));
+  p.max_refine = 40;
+  p.warm_basis = d->warm_start == MSFEM_WARM_USER ? d->warm_basis : nullptr;
+  p.basis_offset = nullptr;
+  p.M = M;
+  p.F = F;
+  p.basis = basis;
+  p.status = cell_status;
+  p.iters = iterations;
+  p.rel_res = reinterpret_cast<double *>(base + kNoallocRelres);
+  p.refinements = reinterpret_cast<int32_t *>(base + kNoallocRefine);
+
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  MSFEM_CUDA(cudaFuncSetAttribute(L.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem));
+  int per_sm = 0, sms = 0;
+  MSFEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, L.fn, L.nt, L.smem));
+  MSFEM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  if (per_sm < 1) return fail(MSFEM_ERR_UNSUPPORTED, "kernel does not fit on an SM");
+  const int grid = std::max(1, std::min(d->n_cells, per_sm * sms));
+  // the counter must start at zero; the per-cell words are overwritten by every cell
+  MSFEM_CUDA(cudaMemsetAsync(p.queue, 0, sizeof(unsigned int), s));
+  void *args[] = {&p};
+  MSFEM_CUDA(cudaLaunchKernel(L.fn, dim3(grid), dim3(L.nt), args, L.smem, s));
+  return MSFEM_OK;
+}
 
 const char *msfem_version(void) { return "msfem_gpu 0.1 (sm_103a)"; }
 
