@@ -206,6 +206,34 @@ int msfem_tabulate_coefficient(msfem_handle *handle,
                                const msfem_batch_desc *desc,
                                int32_t ncomp, double *qp_values);
 
+/* Launch choice for one (dim, N class, precision): which compiled CTA shape
+ * (threads, strip height, CTAs per SM) the batch kernel uses, the FP64
+ * form's residual-check interval and the mixed form's inner FP32 reduction.
+ * No counterpart in the reference (its solver has no launch parameters). */
+typedef struct msfem_tuning {
+  int32_t dim;              /* key */
+  int32_t n_max;            /* key: largest N of the batch (selects the N class) */
+  int32_t precision;        /* key: msfem_precision */
+  int32_t variant;          /* index of the compiled CTA shape */
+  int32_t threads;          /* output: CTA size of that shape */
+  int32_t rows_per_thread;  /* output: strip height (mixed kernels) */
+  int32_t ctas_per_sm;      /* output: occupancy the shape is compiled for */
+  int32_t check_interval;   /* FP64: residual-norm check interval, 0 = adaptive */
+  float inner_tol;          /* MIXED: inner FP32 CG relative reduction */
+  int32_t n_variants;       /* output: compiled shapes for this key */
+  double ms_per_solve;      /* output of msfem_autotune: device time per basis solve */
+} msfem_tuning;
+
+/* Time every compiled shape and parameter choice for desc's key on a prefix
+ * of at most sample_cells cells (the whole batch for uneven N), keep the
+ * fastest in the handle (used by later msfem_run_batch calls with the same
+ * key) and report it in result (nullable). */
+int msfem_autotune(msfem_handle *handle, const msfem_batch_desc *desc,
+                   int32_t sample_cells, msfem_tuning *result);
+
+/* Install a launch choice (e.g. one saved from an earlier msfem_autotune). */
+int msfem_set_tuning(msfem_handle *handle, const msfem_tuning *tuning);
+
 /* Number of doubles msfem_tabulate_coefficient writes for this batch. */
 int64_t msfem_tabulated_size(const msfem_batch_desc *desc, int32_t ncomp);
 

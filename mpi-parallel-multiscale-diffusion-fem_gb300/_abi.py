@@ -104,6 +104,25 @@ class Stats(ctypes.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [
+        ("dim", ctypes.c_int32),
+        ("n_max", ctypes.c_int32),
+        ("precision", ctypes.c_int32),
+        ("variant", ctypes.c_int32),
+        ("threads", ctypes.c_int32),
+        ("rows_per_thread", ctypes.c_int32),
+        ("ctas_per_sm", ctypes.c_int32),
+        ("check_interval", ctypes.c_int32),
+        ("inner_tol", ctypes.c_float),
+        ("n_variants", ctypes.c_int32),
+        ("ms_per_solve", ctypes.c_double),
+    ]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 # Every entry point include/msfem_gpu.h declares: name -> (restype, argtypes)
 EXPORTS = {
     "msfem_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int]),
@@ -116,6 +135,9 @@ EXPORTS = {
     "msfem_tabulate_coefficient": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BatchDesc),
                                                   ctypes.c_int32, ctypes.c_void_p]),
     "msfem_tabulated_size": (ctypes.c_int64, [ctypes.POINTER(BatchDesc), ctypes.c_int32]),
+    "msfem_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BatchDesc), ctypes.c_int32,
+                                      ctypes.POINTER(Tuning)]),
+    "msfem_set_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Tuning)]),
     "msfem_run_batch_noalloc": (ctypes.c_int, [ctypes.POINTER(BatchDesc), ctypes.c_void_p,
                                                ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                ctypes.c_void_p, ctypes.c_void_p]),

@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -58,6 +59,14 @@ struct DevBuf {
   template <typename T> T *as() const { return static_cast<T *>(ptr); }
 };
 
+// Autotuned launch choice for one (dim, N class, precision).
+struct Tune {
+  int variant = 0;
+  int check_interval = 0;
+  float inner_tol = 1e-6f;
+  double ms_per_solve = 0.0;
+};
+
 }  // namespace
 
 struct msfem_handle {
@@ -70,6 +79,8 @@ struct msfem_handle {
   DevBuf corners, nfine, order, queue, qp, qpoff, warm, boff, modes, spheres, sgrid_start, sgrid_ids;
   // outputs staged to the host / internal
   DevBuf M, F, basis, status, iters, relres, refine;
+  // autotuned launch choices, keyed by (dim, N class, precision)
+  std::map<int, Tune> tuning;
 };
 
 namespace msfem {
@@ -269,23 +280,50 @@ struct Launch {
   const void *fn;
   int nt;
   size_t smem;
+  int rows;  // nodes per thread strip (mixed kernels), 0 otherwise
+  int minb;  // CTAs per SM the kernel was compiled for
 };
 
-template <int NMAX, int NT, bool MIXED>
+template <int NMAX, int NT>
 Launch make2d() {
-  return Launch{(const void *)msfem::msfem2d_kernel<NMAX, NT, MIXED>, NT,
-                msfem::Smem2D<NMAX>::bytes(MIXED)};
+  return Launch{(const void *)msfem::msfem2d_kernel<NMAX, NT>, NT, msfem::Smem2D<NMAX>::bytes(false),
+                0, 2};
+}
+template <int NMAX, int NT, int S, int MINB>
+Launch make2d_mixed() {
+  return Launch{(const void *)msfem::msfem2d_mixed_kernel<NMAX, NT, S, MINB>, NT,
+                msfem::Smem2D<NMAX>::bytes(true), S, MINB};
 }
 
-int pick2d(int nmax, bool mixed, Launch *l) {
-  if (nmax <= 16) *l = mixed ? make2d<16, 256, true>() : make2d<16, 128, false>();
-  else if (nmax <= 32) *l = mixed ? make2d<32, 512, true>() : make2d<32, 256, false>();
-  else return -1;
-  return 0;
+// Compiled launch shapes per (dim, N class, precision); index 0 is the default.
+std::vector<Launch> candidates(int dim, int nmax, bool mixed) {
+  if (dim == 2) {
+    if (nmax <= 16) {
+      if (mixed)
+        return {make2d_mixed<16, 128, 2, 2>(), make2d_mixed<16, 64, 4, 4>(),
+                make2d_mixed<16, 128, 2, 1>()};
+      return {make2d<16, 128>()};
+    }
+    if (nmax <= 32) {
+      if (mixed)
+        return {make2d_mixed<32, 256, 4, 2>(), make2d_mixed<32, 256, 4, 1>(),
+                make2d_mixed<32, 512, 2, 1>()};
+      return {make2d<32, 256>()};
+    }
+    return {};
+  }
+  Launch l{};
+  if (msfem::pick3d_kernel(nmax, mixed, &l.fn, &l.nt, &l.smem) != 0) return {};
+  return {l};
 }
 
-int pick3d(int nmax, bool mixed, Launch *l) {
-  return msfem::pick3d_kernel(nmax, mixed, &l->fn, &l->nt, &l->smem);
+int size_class(int dim, int nmax) {
+  if (dim == 2) return nmax <= 16 ? 16 : 32;
+  return nmax <= 8 ? 8 : (nmax <= 16 ? 16 : 24);
+}
+
+int tune_key(int dim, int nmax, bool mixed) {
+  return dim * 1000 + size_class(dim, nmax) * 10 + (mixed ? 1 : 0);
 }
 
 // Sphere hash grid (uniform cells of width >= 2 r_max; each sphere listed in
@@ -508,8 +546,9 @@ int msfem_run_batch_noalloc(const msfem_batch_desc *d, double *M, double *F, dou
     return fail(MSFEM_ERR_INVALID_ARG, "msfem_run_batch_noalloc: M, F and cell_status are required");
   if (d->n_cells == 0) return MSFEM_OK;
   const bool mixed = d->precision == MSFEM_PREC_MIXED;
-  Launch L{};
-  if (pick2d(d->n_fine, mixed, &L) != 0) return fail(MSFEM_ERR_UNSUPPORTED, "no kernel for this N");
+  const std::vector<Launch> cands = candidates(2, d->n_fine, mixed);
+  if (cands.empty()) return fail(MSFEM_ERR_UNSUPPORTED, "no kernel for this N");
+  const Launch L = cands[0];
   int device = 0;
   MSFEM_CUDA(cudaGetDevice(&device));
   void *scratch = nullptr;
@@ -534,7 +573,7 @@ int msfem_run_batch_noalloc(const msfem_batch_desc *d, double *M, double *F, dou
   p.tol = d->tol;
   p.maxit = d->maxit;
   p.check_interval = d->check_interval;
-  p.inner_tol = 1e-4f;
+  p.inner_tol = Tune().inner_tol;
   p.inner_maxit = std::max(1, std::min(d->maxit, 1000));
   p.max_refine = 40;
   p.warm_basis = d->warm_start == MSFEM_WARM_USER ? d->warm_basis : nullptr;
@@ -671,9 +710,14 @@ int msfem_tabulate_coefficient(msfem_handle *h, const msfem_batch_desc *d, int32
   return MSFEM_OK;
 }
 
-int msfem_run_batch(msfem_handle *h, const msfem_batch_desc *d, double *M, double *F,
-                    double *basis, int32_t *cell_status, int32_t *iterations,
-                    msfem_stats *stats) {
+}  // extern "C"
+
+namespace {
+
+// msfem_run_batch with an optional forced launch choice (autotuning).
+int run_batch_impl(msfem_handle *h, const msfem_batch_desc *d, double *M, double *F,
+                   double *basis, int32_t *cell_status, int32_t *iterations,
+                   msfem_stats *stats, const Tune *force) {
   const auto t_start = std::chrono::steady_clock::now();
   if (!h) return fail(MSFEM_ERR_INVALID_ARG, "handle is NULL");
   int rc = validate(d);
@@ -690,10 +734,19 @@ int msfem_run_batch(msfem_handle *h, const msfem_batch_desc *d, double *M, doubl
     nmax = 1;
     for (int c = 0; c < nc; ++c) nmax = std::max(nmax, nf[c]);
   }
-  Launch L{};
-  if ((dim == 2 ? pick2d(nmax, mixed, &L) : pick3d(nmax, mixed, &L)) != 0)
+  const std::vector<Launch> cands = candidates(dim, nmax, mixed);
+  if (cands.empty())
     return fail(MSFEM_ERR_UNSUPPORTED, "no kernel for dim " + std::to_string(dim) + ", N " +
                                            std::to_string(nmax));
+  Tune tn;
+  if (force) {
+    tn = *force;
+  } else {
+    auto it = h->tuning.find(tune_key(dim, nmax, mixed));
+    if (it != h->tuning.end()) tn = it->second;
+  }
+  if (tn.variant < 0 || tn.variant >= (int)cands.size()) tn.variant = 0;
+  const Launch L = cands[tn.variant];
   int64_t h2d = 0, d2h = 0;
   int launches = 0;
 
@@ -737,8 +790,8 @@ int msfem_run_batch(msfem_handle *h, const msfem_batch_desc *d, double *M, doubl
   p.f_value = d->f_value;
   p.tol = d->tol;
   p.maxit = d->maxit;
-  p.check_interval = d->check_interval;
-  p.inner_tol = 1e-4f;
+  p.check_interval = d->check_interval > 0 ? d->check_interval : tn.check_interval;
+  p.inner_tol = tn.inner_tol;
   p.inner_maxit = std::max(1, std::min(d->maxit, 1000));
   p.max_refine = 40;
   p.coef_kind = d->coef.kind;
@@ -904,6 +957,126 @@ int msfem_run_batch(msfem_handle *h, const msfem_batch_desc *d, double *M, doubl
     stats->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count();
   }
   if (nfail) return fail(MSFEM_ERR_NOT_CONVERGED, std::to_string(nfail) + " cell(s) failed; see cell_status");
+  return MSFEM_OK;
+}
+
+void fill_tuning(const Tune &t, int dim, int nmax, int precision, msfem_tuning *out) {
+  const std::vector<Launch> c = candidates(dim, nmax, precision == MSFEM_PREC_MIXED);
+  std::memset(out, 0, sizeof(*out));
+  out->dim = dim;
+  out->n_max = nmax;
+  out->precision = precision;
+  out->variant = t.variant;
+  out->n_variants = (int)c.size();
+  if (t.variant >= 0 && t.variant < (int)c.size()) {
+    out->threads = c[t.variant].nt;
+    out->rows_per_thread = c[t.variant].rows;
+    out->ctas_per_sm = c[t.variant].minb;
+  }
+  out->check_interval = t.check_interval;
+  out->inner_tol = t.inner_tol;
+  out->ms_per_solve = t.ms_per_solve;
+}
+
+}  // namespace
+
+extern "C" {
+
+int msfem_run_batch(msfem_handle *h, const msfem_batch_desc *d, double *M, double *F,
+                    double *basis, int32_t *cell_status, int32_t *iterations,
+                    msfem_stats *stats) {
+  return run_batch_impl(h, d, M, F, basis, cell_status, iterations, stats, nullptr);
+}
+
+int msfem_set_tuning(msfem_handle *h, const msfem_tuning *t) {
+  if (!h || !t) return fail(MSFEM_ERR_INVALID_ARG, "handle and tuning are required");
+  if (t->dim != 2 && t->dim != 3) return fail(MSFEM_ERR_INVALID_ARG, "tuning dim must be 2 or 3");
+  const bool mixed = t->precision == MSFEM_PREC_MIXED;
+  const std::vector<Launch> c = candidates(t->dim, t->n_max, mixed);
+  if (t->variant < 0 || t->variant >= (int)c.size())
+    return fail(MSFEM_ERR_INVALID_ARG, "tuning variant out of range");
+  if (t->check_interval < 0 || !(t->inner_tol > 0.0f && t->inner_tol < 1.0f))
+    return fail(MSFEM_ERR_INVALID_ARG, "tuning parameters out of range");
+  Tune tn;
+  tn.variant = t->variant;
+  tn.check_interval = t->check_interval;
+  tn.inner_tol = t->inner_tol;
+  tn.ms_per_solve = t->ms_per_solve;
+  h->tuning[tune_key(t->dim, t->n_max, mixed)] = tn;
+  return MSFEM_OK;
+}
+
+int msfem_autotune(msfem_handle *h, const msfem_batch_desc *d, int32_t sample_cells,
+                   msfem_tuning *result) {
+  if (!h) return fail(MSFEM_ERR_INVALID_ARG, "handle is NULL");
+  int rc = validate(d);
+  if (rc) return rc;
+  if (d->n_cells < 1) return fail(MSFEM_ERR_INVALID_ARG, "autotune needs at least one cell");
+  MSFEM_CUDA(cudaSetDevice(h->device));
+  std::vector<int32_t> nf;
+  if ((rc = host_nfine(h, d, nf))) return rc;
+  int nmax = d->n_fine;
+  if (d->n_fine_per_cell) nmax = *std::max_element(nf.begin(), nf.end());
+  const bool mixed = d->precision == MSFEM_PREC_MIXED;
+  const std::vector<Launch> cands = candidates(d->dim, nmax, mixed);
+  if (cands.empty()) return fail(MSFEM_ERR_UNSUPPORTED, "no kernel for this size");
+  // sample: a prefix of the cells (uniform N without caller offsets), else the batch
+  msfem_batch_desc s = *d;
+  if (!d->n_fine_per_cell && !d->coef.qp_offset && sample_cells > 0)
+    s.n_cells = std::min(d->n_cells, sample_cells);
+  if (d->warm_start == MSFEM_WARM_USER) s.warm_start = MSFEM_WARM_NONE;
+  const int nv = 1 << d->dim, nc = s.n_cells;
+  const bool dev = d->memory == MSFEM_MEM_DEVICE;
+  std::vector<double> Mh, Fh;
+  double *Mp = nullptr, *Fp = nullptr;
+  if (dev) {
+    MSFEM_CUDA(h->M.ensure(sizeof(double) * nc * nv * nv));
+    MSFEM_CUDA(h->F.ensure(sizeof(double) * nc * nv));
+    Mp = h->M.as<double>();
+    Fp = h->F.as<double>();
+  } else {
+    Mh.resize((size_t)nc * nv * nv);
+    Fh.resize((size_t)nc * nv);
+    Mp = Mh.data();
+    Fp = Fh.data();
+  }
+  std::vector<Tune> trials;
+  for (int v = 0; v < (int)cands.size(); ++v) {
+    if (mixed) {
+      for (float it : {1e-4f, 1e-5f, 1e-6f, 1e-7f}) {
+        Tune t;
+        t.variant = v;
+        t.inner_tol = it;
+        trials.push_back(t);
+      }
+    } else {
+      for (int ci : {0, 1, 4}) {
+        Tune t;
+        t.variant = v;
+        t.check_interval = ci;
+        trials.push_back(t);
+      }
+    }
+  }
+  Tune best;
+  double best_ms = 1e300;
+  for (Tune &t : trials) {
+    msfem_stats st;
+    double ms = 1e300;
+    for (int rep = 0; rep < 2; ++rep) {
+      rc = run_batch_impl(h, &s, Mp, Fp, nullptr, nullptr, nullptr, &st, &t);
+      if (rc != MSFEM_OK && rc != MSFEM_ERR_NOT_CONVERGED) return rc;
+      if (st.cells_failed == 0) ms = std::min(ms, st.kernel_ms);
+    }
+    t.ms_per_solve = ms / std::max<int64_t>(1, (int64_t)nc * nv);
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = t;
+    }
+  }
+  if (best_ms >= 1e300) return fail(MSFEM_ERR_NOT_CONVERGED, "no launch choice converged on the sample");
+  h->tuning[tune_key(d->dim, nmax, mixed)] = best;
+  if (result) fill_tuning(best, d->dim, nmax, d->precision, result);
   return MSFEM_OK;
 }
 

@@ -1,4 +1,4 @@
-// msfem_kernel2d.cuh -- 2D multiscale-basis kernel for sm_103a.
+// msfem_kernel2d.cuh -- 2D multiscale-basis kernels for sm_103a.
 //
 // One CTA owns one coarse cell at a time (persistent CTAs pull cells from a
 // work queue).  Per cell, entirely in shared memory:
@@ -11,19 +11,20 @@
 //      basis_q1.tpp), with a per-RHS relative l2 stopping rule;
 //   4. epilogue M_ij = phi_i^T A phi_j and F_i = phi_i^T b over all fine nodes
 //      (diffusion_problem_basis.tpp:245-285) -- in scaled form
-//      M_ij = phi~_i^T A~ phi~_j with phi~ = D^1/2 phi.
+//      M_ij = phi~_i^T A~ phi~_j,  phi~ = D^1/2 phi,  F_i = phi~_i^T D^-1/2 b.
 //
-// Precision forms:
-//   FP64  : plain FP64 CG (the drop-in form).
-//   MIXED : FP64 outer loop  r = b - A x  (true FP64 residual), inner FP32 CG
-//           on A~ d = r to a relative reduction, x += d in FP64.
+// Kernels:
+//   msfem2d_kernel        plain FP64 CG (the drop-in form); bound by the FP64 pipe.
+//   msfem2d_mixed_kernel  FP64 outer loop r = b - A x (true FP64 residual),
+//                         inner FP32 CG on A~ d = r, x += d in FP64.  Threads
+//                         own vertical strips of S nodes (register blocking).
 //
 // Shared-memory layout (node-major, 4 values per node; P = N + 3: the
 // (N+1)^2 node grid plus a zero ring, node (ix,iy) at (iy+1) P + ix + 1):
 //   c64 [G][4]  scaled couplings E, NE, N, NW of each node (FP64)
 //   v64 [G][4]  FP64 work vector of the 4 RHS (p~ in FP64 CG, phi~ otherwise)
-//   s64 [G]     D^-1/2,  d64 [G] D (diagonal),  bl64 [G] D^-1/2 b_load
-//   c32 [G][4], v32 [G][4]   FP32 copies for the MIXED inner loop
+//   d64 [G]     diagonal D (D^-1/2 is recomputed where needed)
+//   v32 [G][4]  FP32 search direction of the mixed inner loop
 #pragma once
 
 #include "msfem_common.cuh"
@@ -38,15 +39,12 @@ struct Smem2D {
   static constexpr size_t al(size_t x) { return (x + 127) & ~size_t(127); }
   static constexpr size_t kC64 = 0;
   static constexpr size_t kV64 = al(kC64 + sizeof(double) * 4 * G);
-  static constexpr size_t kS64 = al(kV64 + sizeof(double) * 4 * G);
-  static constexpr size_t kD64 = al(kS64 + sizeof(double) * G);
-  static constexpr size_t kB64 = al(kD64 + sizeof(double) * G);
-  static constexpr size_t kEndFP64 = al(kB64 + sizeof(double) * G);
-  static constexpr size_t kC32 = kEndFP64;
-  static constexpr size_t kV32 = al(kC32 + sizeof(float) * 4 * G);
+  static constexpr size_t kD64 = al(kV64 + sizeof(double) * 4 * G);
+  static constexpr size_t kEndFP64 = al(kD64 + sizeof(double) * G);
+  static constexpr size_t kV32 = kEndFP64;
   static constexpr size_t kEndMixed = al(kV32 + sizeof(float) * 4 * G);
   static constexpr size_t bytes(bool mixed) { return mixed ? kEndMixed : kEndFP64; }
-  static_assert(kV64 % 16 == 0 && kC32 % 16 == 0 && kV32 % 16 == 0, "vector alignment");
+  static_assert(kV64 % 16 == 0 && kV32 % 16 == 0, "vector alignment");
 };
 
 __device__ __forceinline__ void ld4(const double *__restrict__ v, int g, double (&t)[4]) {
@@ -94,7 +92,7 @@ __device__ __forceinline__ void stencil9(const T *__restrict__ c, const T *__res
 // Warp 0 finishes a K-value block reduction: red holds NW*K warp partials
 // ([warp][value]); on return lane l holds the block total of value l % K.
 template <int K, typename T>
-__device__ __forceinline__ T warp0_finish(const T *red, int NW, int lane) {
+__device__ __forceinline__ T warp_finish(const T *red, int NW, int lane) {
   T s = T(0);
   for (int i = lane; i < NW * K; i += 32) s += red[i];
 #pragma unroll
@@ -116,15 +114,15 @@ struct CellShared2D {
   double q1coef[16];
   double q1shift[2];
   double q1iscale;
-  double jinv_g[9];   // affine cells: G = w|det| Jinv A Jinv^T as 3x3 map (a11,a12,a22) -> (G11,G12,G22)
-  double jfine[4];    // affine cells: fine-cell Jacobian (column-major dx/dxi, dx/deta)
+  double jinv_g[9];   // affine cells: (a11,a12,a22) -> w|det| Jinv A Jinv^T as (G11,G12,G22)
+  double jfine[4];    // affine cells: fine-cell Jacobian, columns dx/dxi, dx/deta
   double absdet;      // affine cells: |det J_fine|
   double bb[4];       // ||b_i||^2 (unscaled)
+  double nu[4];       // last ||r_i||^2 (unscaled)
   double rho[4];
   double alpha[4];
   double beta[4];
   double dmin;
-  float alpha32[4];
   int active[4];
   int iters[4];
   int status;
@@ -151,8 +149,410 @@ __device__ __forceinline__ double lval(int b, int qb) {
   return b ? gauss2(qb) : gauss2(1 - qb);
 }
 
-template <int NMAX, int NT, bool MIXED>
-__global__ void __launch_bounds__(NT, MIXED ? 1 : 2)
+__device__ __forceinline__ double qnan() { return __longlong_as_double(0x7ff8000000000000ll); }
+
+// Boundary node k in [0, 4N): walk around the cell boundary.
+__device__ __forceinline__ void boundary_node(int k, int N, int &ix, int &iy) {
+  if (k < N) { ix = k; iy = 0; }
+  else if (k < 2 * N) { ix = N; iy = k - N; }
+  else if (k < 3 * N) { ix = N - (k - 2 * N); iy = N; }
+  else { ix = 0; iy = N - (k - 3 * N); }
+}
+
+// ---------------------------------------------------------------------------
+// Shared per-cell phases
+// ---------------------------------------------------------------------------
+
+// Geometry, Q1 data, zeroed arrays.  Returns the cell status.
+template <int NMAX, int NT>
+__device__ int cell_begin(const KernelParams &p, CellShared2D &cs, int cell, int N,
+                          double *c64, double *v64, double *d64, float *v32, int tid) {
+  const int P = N + 3, G = P * P;
+  if (tid < 8) cs.corners[tid] = p.corners[(int64_t)cell * 8 + tid];
+  for (int i = tid; i < 4 * G; i += NT) { c64[i] = 0.0; v64[i] = 0.0; }
+  for (int i = tid; i < G; i += NT) d64[i] = 0.0;
+  if (v32)
+    for (int i = tid; i < 4 * G; i += NT) v32[i] = 0.0f;
+  if (tid < 4) { cs.iters[tid] = 0; cs.active[tid] = 1; cs.nu[tid] = 0.0; }
+  __syncthreads();
+  if (tid == 0) {
+    const double *cr = cs.corners;
+    int st = MSFEM_CELL_CONVERGED;
+    if (N < 1 || N > NMAX) st = MSFEM_CELL_BAD_INPUT;
+    if (st == MSFEM_CELL_CONVERGED && !q1_setup<2>(cr, cs.q1coef, cs.q1shift, &cs.q1iscale))
+      st = MSFEM_CELL_BAD_INPUT;
+    // parallelogram test v0 + v3 == v1 + v2 (exact)
+    const int aff = (cr[0] + cr[6] == cr[2] + cr[4]) && (cr[1] + cr[7] == cr[3] + cr[5]);
+    cs.affine = aff;
+    cs.refinements = 0;
+    if (aff && st == MSFEM_CELL_CONVERGED) {
+      const double invN = 1.0 / (double)N;
+      const double J00 = (cr[2] - cr[0]) * invN, J10 = (cr[3] - cr[1]) * invN;
+      const double J01 = (cr[4] - cr[0]) * invN, J11 = (cr[5] - cr[1]) * invN;
+      const double det = J00 * J11 - J01 * J10;
+      if (!(det > 0.0)) st = MSFEM_CELL_BAD_INPUT;
+      const double id = 1.0 / det;
+      const double i00 = J11 * id, i01 = -J01 * id, i10 = -J10 * id, i11 = J00 * id;
+      const double w = 0.25 * fabs(det);
+      // G = w Ji A Ji^T,  A = [[a11,a12],[a12,a22]]
+      cs.jinv_g[0] = w * i00 * i00; cs.jinv_g[1] = w * 2.0 * i00 * i01; cs.jinv_g[2] = w * i01 * i01;
+      cs.jinv_g[3] = w * i00 * i10; cs.jinv_g[4] = w * (i00 * i11 + i01 * i10); cs.jinv_g[5] = w * i01 * i11;
+      cs.jinv_g[6] = w * i10 * i10; cs.jinv_g[7] = w * 2.0 * i10 * i11; cs.jinv_g[8] = w * i11 * i11;
+      cs.jfine[0] = J00; cs.jfine[1] = J10; cs.jfine[2] = J01; cs.jfine[3] = J11;
+      cs.absdet = fabs(det);
+    }
+    cs.status = st;
+  }
+  __syncthreads();
+  return cs.status;
+}
+
+// Malformed cell: NaN outputs and the status word, then move on.
+__device__ void cell_report_bad(const KernelParams &p, const CellShared2D &cs, int cell, int tid) {
+  if (tid < 16) p.M[(int64_t)cell * 16 + tid] = qnan();
+  if (tid < 4) {
+    p.F[(int64_t)cell * 4 + tid] = qnan();
+    if (p.iters) p.iters[(int64_t)cell * 4 + tid] = 0;
+  }
+  if (tid == 0) {
+    p.status[cell] = cs.status;
+    if (p.rel_res) p.rel_res[cell] = qnan();
+    if (p.refinements) p.refinements[cell] = 0;
+  }
+}
+
+// QGauss(2) element matrix of fine cell (cx, cy): diagonal Kd[4] and the
+// six couplings Ko = (K01, K02, K03, K12, K13, K23).  Returns false for an
+// inverted fine cell.
+__device__ __forceinline__ bool element2d(const KernelParams &p, const CellShared2D &cs,
+                                          const double *__restrict__ tab, int N, int cx, int cy,
+                                          bool need_x, double (&Kd)[4], double (&Ko)[6]) {
+  const int nfc = N * N, fc = cx + N * cy;
+  if (cs.affine) {
+    // G_q = w|det| Jinv A_q Jinv^T, then moments of the tensor-product Q1
+    // gradients: d psi/d xi depends on eta only and d psi/d eta on xi only.
+    double G11[4], G12[4], G22[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      double xq[2] = {0.0, 0.0}, A[3];
+      if (need_x) {
+        const double u = cx + gauss2(q & 1), v = cy + gauss2(q >> 1);
+        xq[0] = cs.corners[0] + cs.jfine[0] * u + cs.jfine[2] * v;
+        xq[1] = cs.corners[1] + cs.jfine[1] * u + cs.jfine[3] * v;
+      }
+      coef_at<2>(p, xq, tab, q, nfc, fc, A);
+      G11[q] = cs.jinv_g[0] * A[0] + cs.jinv_g[1] * A[1] + cs.jinv_g[2] * A[2];
+      G12[q] = cs.jinv_g[3] * A[0] + cs.jinv_g[4] * A[1] + cs.jinv_g[5] * A[2];
+      G22[q] = cs.jinv_g[6] * A[0] + cs.jinv_g[7] * A[1] + cs.jinv_g[8] * A[2];
+    }
+    const double Ay[2] = {G11[0] + G11[1], G11[2] + G11[3]};  // sum over qx
+    const double Bx[2] = {G22[0] + G22[2], G22[1] + G22[3]};  // sum over qy
+    double Pyy[2][2], Pxx[2][2], Q[2][2];
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+      for (int b = 0; b < 2; ++b) {
+        Pyy[a][b] = Ay[0] * (lval(a, 0) * lval(b, 0)) + Ay[1] * (lval(a, 1) * lval(b, 1));
+        Pxx[a][b] = Bx[0] * (lval(a, 0) * lval(b, 0)) + Bx[1] * (lval(a, 1) * lval(b, 1));
+        double s = 0.0;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) s = fma(G12[q], lval(a, q >> 1) * lval(b, q & 1), s);
+        Q[a][b] = s;  // a: y-index (of eta), b: x-index (of xi)
+      }
+    auto Kij = [&](int i, int j) {
+      const int ix = i & 1, iy = i >> 1, jx = j & 1, jy = j >> 1;
+      const double sxi = ix ? 1.0 : -1.0, syi = iy ? 1.0 : -1.0;
+      const double sxj = jx ? 1.0 : -1.0, syj = jy ? 1.0 : -1.0;
+      return (sxi * sxj) * Pyy[iy][jy] + (syi * syj) * Pxx[ix][jx] + (sxi * syj) * Q[iy][jx] +
+             (syi * sxj) * Q[jy][ix];
+    };
+#pragma unroll
+    for (int i = 0; i < 4; ++i) Kd[i] = Kij(i, i);
+    Ko[0] = Kij(0, 1); Ko[1] = Kij(0, 2); Ko[2] = Kij(0, 3);
+    Ko[3] = Kij(1, 2); Ko[4] = Kij(1, 3); Ko[5] = Kij(2, 3);
+    return true;
+  }
+  // general bilinear cell: per-Gauss-point Jacobian
+  const double invN = 1.0 / (double)N;
+  double V[8];
+  bilinear_map(cs.corners, cx * invN, cy * invN, V + 0);
+  bilinear_map(cs.corners, (cx + 1) * invN, cy * invN, V + 2);
+  bilinear_map(cs.corners, cx * invN, (cy + 1) * invN, V + 4);
+  bilinear_map(cs.corners, (cx + 1) * invN, (cy + 1) * invN, V + 6);
+  double K[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) K[i][j] = 0.0;
+  bool ok = true;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int qx = q & 1, qy = q >> 1;
+    double J00 = 0, J01 = 0, J10 = 0, J11 = 0, xq[2] = {0.0, 0.0};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int kx = k & 1, ky = k >> 1;
+      const double gx = (kx ? 1.0 : -1.0) * lval(ky, qy);
+      const double gy = (ky ? 1.0 : -1.0) * lval(kx, qx);
+      const double psi = lval(kx, qx) * lval(ky, qy);
+      J00 += V[2 * k] * gx; J01 += V[2 * k] * gy;
+      J10 += V[2 * k + 1] * gx; J11 += V[2 * k + 1] * gy;
+      xq[0] += psi * V[2 * k]; xq[1] += psi * V[2 * k + 1];
+    }
+    const double det = J00 * J11 - J01 * J10;
+    if (!(det > 0.0)) ok = false;
+    const double id = 1.0 / det;
+    const double i00 = J11 * id, i01 = -J01 * id, i10 = -J10 * id, i11 = J00 * id;
+    const double w = 0.25 * fabs(det);
+    double A[3];
+    coef_at<2>(p, xq, tab, q, nfc, fc, A);
+    const double t00 = i00 * A[0] + i01 * A[1], t01 = i00 * A[1] + i01 * A[2];
+    const double t10 = i10 * A[0] + i11 * A[1], t11 = i10 * A[1] + i11 * A[2];
+    const double Gm0 = w * (t00 * i00 + t01 * i01);
+    const double Gm1 = w * (t00 * i10 + t01 * i11);
+    const double Gm2 = w * (t10 * i10 + t11 * i11);
+    double gx[4], gy[4], ax[4], ay[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int kx = k & 1, ky = k >> 1;
+      gx[k] = (kx ? 1.0 : -1.0) * lval(ky, qy);
+      gy[k] = (ky ? 1.0 : -1.0) * lval(kx, qx);
+      ax[k] = Gm0 * gx[k] + Gm1 * gy[k];
+      ay[k] = Gm1 * gx[k] + Gm2 * gy[k];
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = i; j < 4; ++j) K[i][j] = fma(gx[i], ax[j], fma(gy[i], ay[j], K[i][j]));
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) Kd[i] = K[i][i];
+  Ko[0] = K[0][1]; Ko[1] = K[0][2]; Ko[2] = K[0][3];
+  Ko[3] = K[1][2]; Ko[4] = K[1][3]; Ko[5] = K[2][3];
+  return ok;
+}
+
+// Assembly: 4-colour scatter of the element matrices into the node stencil.
+template <int NT>
+__device__ void assemble2d(const KernelParams &p, CellShared2D &cs, int cell, int N,
+                           double *c64, double *d64, int tid) {
+  const int P = N + 3, nfc = N * N;
+  const double *tab = nullptr;
+  if (p.coef_kind == MSFEM_COEF_TABULATED)
+    tab = p.qp_values + (p.qp_offset ? p.qp_offset[cell] : (int64_t)cell * p.ncomp * 4 * nfc);
+  const bool need_x = p.coef_kind != MSFEM_COEF_TABULATED && p.coef_kind != MSFEM_COEF_CONSTANT;
+  for (int col = 0; col < 4; ++col) {
+    const int ox = col & 1, oy = col >> 1;
+    const int nx = (N - ox + 1) >> 1, ny = (N - oy + 1) >> 1;
+    for (int idx = tid; idx < nx * ny; idx += NT) {
+      const int cx = ox + 2 * (idx % nx), cy = oy + 2 * (idx / nx);
+      double Kd[4], Ko[6];
+      if (!element2d(p, cs, tab, N, cx, cy, need_x, Kd, Ko)) cs.status = MSFEM_CELL_BAD_INPUT;
+      const int g0 = (cy + 1) * P + cx + 1;
+      const int g1 = g0 + 1, g2 = g0 + P, g3 = g0 + P + 1;
+      d64[g0] += Kd[0]; d64[g1] += Kd[1]; d64[g2] += Kd[2]; d64[g3] += Kd[3];
+      c64[4 * g0 + 0] += Ko[0];  // E  of node 0 (0-1)
+      c64[4 * g2 + 0] += Ko[5];  // E  of node 2 (2-3)
+      c64[4 * g0 + 2] += Ko[1];  // N  of node 0 (0-2)
+      c64[4 * g1 + 2] += Ko[4];  // N  of node 1 (1-3)
+      c64[4 * g0 + 1] += Ko[2];  // NE of node 0 (0-3)
+      c64[4 * g1 + 3] += Ko[3];  // NW of node 1 (1-2)
+    }
+    __syncthreads();
+  }
+}
+
+// Symmetric scaling and Dirichlet data.  After it: c64 holds the scaled
+// couplings, v64 holds phi~ = D^1/2 g_i on the boundary and 0 inside, and
+// cs.dmin the smallest interior diagonal.  red needs NW doubles.
+template <int NT>
+__device__ void scale2d(CellShared2D &cs, int N, double *c64, double *v64, const double *d64,
+                        double *red, int tid) {
+  constexpr int NW = NT / 32;
+  const int P = N + 3, n = N + 1, lane = tid & 31, warp = tid >> 5;
+  // D^-1/2 into v64[.][0] (temporary)
+  double dmin_part = 1e300;
+  for (int k = tid; k < n * n; k += NT) {
+    const int ix = k % n, iy = k / n;
+    const int g = (iy + 1) * P + ix + 1;
+    const double d = d64[g];
+    v64[4 * g] = rsqrt(d);
+    if (ix > 0 && iy > 0 && ix < N && iy < N) {
+      dmin_part = fmin(dmin_part, d);
+      if (!(d > 0.0) || !isfinite(d)) cs.status = MSFEM_CELL_NAN;
+    }
+  }
+  __syncthreads();
+  for (int k = tid; k < n * n; k += NT) {
+    const int g = (k / n + 1) * P + k % n + 1;
+    const double s = v64[4 * g];
+    double cc[4];
+    ld4(c64, g, cc);
+    cc[0] *= s * v64[4 * (g + 1)];
+    cc[1] *= s * v64[4 * (g + P + 1)];
+    cc[2] *= s * v64[4 * (g + P)];
+    cc[3] *= s * v64[4 * (g + P - 1)];
+    st4(c64, g, cc);
+  }
+#pragma unroll
+  for (int m = 16; m >= 1; m >>= 1) dmin_part = fmin(dmin_part, shfl_xor_d(dmin_part, m));
+  if (lane == 0) red[warp] = dmin_part;
+  __syncthreads();
+  // Dirichlet data phi~_i = D^1/2 g_i (BasisQ1 at the node); interior 0
+  for (int k = tid; k < n * n; k += NT) {
+    const int ix = k % n, iy = k / n;
+    const int g = (iy + 1) * P + ix + 1;
+    double t[4] = {0.0, 0.0, 0.0, 0.0};
+    if (ix == 0 || iy == 0 || ix == N || iy == N) {
+      double x[2], gv[4];
+      bilinear_map(cs.corners, ix / (double)N, iy / (double)N, x);
+      q1_eval<2>(cs.q1coef, cs.q1shift, cs.q1iscale, x, gv);
+      const double sq = d64[g] * v64[4 * g];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) t[r] = gv[r] * sq;
+    }
+    st4(v64, g, t);
+  }
+  if (tid == 0) {
+    double m = 1e300;
+    for (int w = 0; w < NW; ++w) m = fmin(m, red[w]);
+    cs.dmin = m;
+  }
+  __syncthreads();
+}
+
+// Scaled boundary value phi~ at boundary node (ix, iy).
+__device__ __forceinline__ void boundary_value(const CellShared2D &cs, const double *d64, int N,
+                                               int P, int ix, int iy, double (&t)[4]) {
+  const int g = (iy + 1) * P + ix + 1;
+  double x[2], gv[4];
+  bilinear_map(cs.corners, ix / (double)N, iy / (double)N, x);
+  q1_eval<2>(cs.q1coef, cs.q1shift, cs.q1iscale, x, gv);
+  const double d = d64[g];
+  const double sq = d * rsqrt(d);
+#pragma unroll
+  for (int r = 0; r < 4; ++r) t[r] = gv[r] * sq;
+}
+
+// Load vector b_k = f int psi_k at node (ix, iy).  Affine cells: every fine
+// cell carries f |det| / 4 to each of its vertices; general cells: QGauss(2)
+// over the adjacent fine cells.
+__device__ double node_load(const KernelParams &p, const CellShared2D &cs, int N, int ix, int iy) {
+  if (cs.affine) {
+    const double m = (ix == 0 || ix == N ? 1.0 : 2.0) * (iy == 0 || iy == N ? 1.0 : 2.0);
+    return p.f_value * 0.25 * cs.absdet * m;
+  }
+  const double invN = 1.0 / (double)N;
+  double b = 0.0;
+  for (int dy = -1; dy <= 0; ++dy)
+    for (int dx = -1; dx <= 0; ++dx) {
+      const int cx = ix + dx, cy = iy + dy;
+      if (cx < 0 || cy < 0 || cx >= N || cy >= N) continue;
+      const int kx = ix - cx, ky = iy - cy;  // local vertex of the node
+      double V[8];
+      bilinear_map(cs.corners, cx * invN, cy * invN, V + 0);
+      bilinear_map(cs.corners, (cx + 1) * invN, cy * invN, V + 2);
+      bilinear_map(cs.corners, cx * invN, (cy + 1) * invN, V + 4);
+      bilinear_map(cs.corners, (cx + 1) * invN, (cy + 1) * invN, V + 6);
+      for (int q = 0; q < 4; ++q) {
+        const int qx = q & 1, qy = q >> 1;
+        double J00 = 0, J01 = 0, J10 = 0, J11 = 0;
+        for (int k = 0; k < 4; ++k) {
+          const int vx = k & 1, vy = k >> 1;
+          const double gx = (vx ? 1.0 : -1.0) * lval(vy, qy);
+          const double gy = (vy ? 1.0 : -1.0) * lval(vx, qx);
+          J00 += V[2 * k] * gx; J01 += V[2 * k] * gy;
+          J10 += V[2 * k + 1] * gx; J11 += V[2 * k + 1] * gy;
+        }
+        b += lval(kx, qx) * lval(ky, qy) * 0.25 * fabs(J00 * J11 - J01 * J10);
+      }
+    }
+  return p.f_value * b;
+}
+
+// Epilogue contribution of node (ix, iy) with y = A~ phi~ known there.
+__device__ __forceinline__ void epilogue_node(const KernelParams &p, const CellShared2D &cs,
+                                              const double *d64, int N, int P, int ix, int iy,
+                                              const double (&ph)[4], const double (&y)[4],
+                                              double (&acc)[32]) {
+  const int g = (iy + 1) * P + ix + 1;
+  const double bl = node_load(p, cs, N, ix, iy) * rsqrt(d64[g]);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[4 * i + j] = fma(ph[i], y[j], acc[4 * i + j]);
+    acc[16 + i] = fma(ph[i], bl, acc[16 + i]);
+  }
+}
+
+// Final block reduction of the 32 epilogue values and the output writes.
+// acc: M (16), F (4), interior ||A phi||^2 (4) unless use_nu, then cs.nu.
+template <int NT, bool MIXED>
+__device__ void epilogue_finish(const KernelParams &p, CellShared2D &cs, int cell, double (&acc)[32],
+                                double *red32v, bool use_nu, const int (&total_iters)[4], int tid) {
+  constexpr int NW = NT / 32;
+  const int lane = tid & 31, warp = tid >> 5;
+  const double tot = warp_transpose_reduce<32>(acc, lane);
+  red32v[warp * 32 + lane] = tot;
+  __syncthreads();
+  if (warp == 0) {
+    double s = 0.0;
+    for (int w = 0; w < NW; ++w) s += red32v[w * 32 + lane];
+    if (lane < 16) p.M[(int64_t)cell * 16 + lane] = s;
+    else if (lane < 20) p.F[(int64_t)cell * 4 + (lane - 16)] = s;
+    double rel = 0.0;
+    if (lane >= 20 && lane < 24) {
+      const double bb = cs.bb[lane - 20];
+      const double nu = use_nu ? cs.nu[lane - 20] : s;
+      rel = bb > 0.0 ? sqrt(nu / bb) : sqrt(nu);
+    }
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) rel = fmax(rel, shfl_xor_d(rel, m));
+    if (lane < 4 && p.iters) {
+      const int itv = cs.iters[lane];
+      int out;
+      if (MIXED) out = total_iters[lane];
+      else out = itv >= 0 ? itv : (itv <= -1000000 ? -itv - 1000000 : -itv);
+      p.iters[(int64_t)cell * 4 + lane] = out;
+    }
+    if (lane == 0) {
+      int st = cs.status;  // MSFEM_CELL_NAN when a diagonal was not positive
+      for (int r = 0; r < 4; ++r) {
+        const int itv = cs.iters[r];
+        if (itv <= -1000000) st = st == MSFEM_CELL_CONVERGED ? MSFEM_CELL_MAXIT : st;
+        else if (itv < 0) st = MSFEM_CELL_NAN;
+      }
+      if (!isfinite(rel)) st = MSFEM_CELL_NAN;
+      p.status[cell] = st;
+      if (p.rel_res) p.rel_res[cell] = rel;
+      if (p.refinements) p.refinements[cell] = cs.refinements;
+    }
+  }
+  __syncthreads();
+}
+
+// Basis output phi = D^-1/2 phi~ (lexicographic nodes), when requested.
+template <int NT>
+__device__ void write_basis(const KernelParams &p, int cell, int N, const double *v64,
+                            const double *d64, int tid) {
+  if (!p.basis) return;
+  const int P = N + 3, n = N + 1;
+  double *out = p.basis + (p.basis_offset ? p.basis_offset[cell] : (int64_t)cell * 4 * n * n);
+  for (int k = tid; k < n * n; k += NT) {
+    const int g = (k / n + 1) * P + k % n + 1;
+    double ph[4];
+    ld4(v64, g, ph);
+    const double s = rsqrt(d64[g]);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) out[(int64_t)i * n * n + k] = ph[i] * s;
+  }
+}
+
+// ===========================================================================
+// Plain FP64 form
+// ===========================================================================
+template <int NMAX, int NT>
+__global__ void __launch_bounds__(NT, 2)
 msfem2d_kernel(const KernelParams p) {
   using L = Smem2D<NMAX>;
   constexpr int NW = NT / 32;
@@ -160,16 +560,13 @@ msfem2d_kernel(const KernelParams p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double *c64 = reinterpret_cast<double *>(smem_raw + L::kC64);
   double *v64 = reinterpret_cast<double *>(smem_raw + L::kV64);
-  double *s64 = reinterpret_cast<double *>(smem_raw + L::kS64);
   double *d64 = reinterpret_cast<double *>(smem_raw + L::kD64);
-  double *b64 = reinterpret_cast<double *>(smem_raw + L::kB64);
-  float *c32 = reinterpret_cast<float *>(smem_raw + L::kC32);
-  float *v32 = reinterpret_cast<float *>(smem_raw + L::kV32);
   __shared__ CellShared2D cs;
-  __shared__ double red[2][NW * 32];
-  __shared__ float red32[2][NW * 8];
+  __shared__ double red[2][NW * 8];
+  __shared__ double redE[NW * 32];
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int zero_iters[4] = {0, 0, 0, 0};
 
   for (;;) {
     if (tid == 0) {
@@ -180,231 +577,20 @@ msfem2d_kernel(const KernelParams p) {
     const int cell = cs.cell;
     if (cell < 0) break;
     const int N = p.n_fine ? p.n_fine[cell] : p.n_fine_uniform;
-    const int P = N + 3, G = P * P, n = N + 1, nI = (N - 1) * (N - 1);
+    const int P = N + 3, n = N + 1, nI = (N - 1) * (N - 1);
 
-    // ---------------- set-up -------------------------------------------
-    if (tid < 8) cs.corners[tid] = p.corners[(int64_t)cell * 8 + tid];
-    for (int i = tid; i < 4 * G; i += NT) { c64[i] = 0.0; v64[i] = 0.0; }
-    for (int i = tid; i < G; i += NT) { s64[i] = 0.0; d64[i] = 0.0; b64[i] = 0.0; }
-    if (MIXED)
-      for (int i = tid; i < 4 * G; i += NT) { c32[i] = 0.0f; v32[i] = 0.0f; }
-    if (tid < 4) { cs.iters[tid] = 0; cs.active[tid] = 1; }
-    __syncthreads();
-    if (tid == 0) {
-      const double *cr = cs.corners;
-      int st = MSFEM_CELL_CONVERGED;
-      if (N < 1 || N > NMAX) st = MSFEM_CELL_BAD_INPUT;
-      if (!q1_setup<2>(cr, cs.q1coef, cs.q1shift, &cs.q1iscale)) st = MSFEM_CELL_BAD_INPUT;
-      // parallelogram test v0 + v3 == v1 + v2 (exact)
-      const int aff = (cr[0] + cr[6] == cr[2] + cr[4]) && (cr[1] + cr[7] == cr[3] + cr[5]);
-      cs.affine = aff;
-      if (aff && st == MSFEM_CELL_CONVERGED) {
-        const double invN = 1.0 / (double)N;
-        const double J00 = (cr[2] - cr[0]) * invN, J10 = (cr[3] - cr[1]) * invN;
-        const double J01 = (cr[4] - cr[0]) * invN, J11 = (cr[5] - cr[1]) * invN;
-        const double det = J00 * J11 - J01 * J10;
-        if (!(det > 0.0)) st = MSFEM_CELL_BAD_INPUT;
-        const double id = 1.0 / det;
-        const double i00 = J11 * id, i01 = -J01 * id, i10 = -J10 * id, i11 = J00 * id;
-        const double w = 0.25 * fabs(det);
-        // G = w Ji A Ji^T,  A = [[a11,a12],[a12,a22]]
-        cs.jinv_g[0] = w * i00 * i00; cs.jinv_g[1] = w * 2.0 * i00 * i01; cs.jinv_g[2] = w * i01 * i01;
-        cs.jinv_g[3] = w * i00 * i10; cs.jinv_g[4] = w * (i00 * i11 + i01 * i10); cs.jinv_g[5] = w * i01 * i11;
-        cs.jinv_g[6] = w * i10 * i10; cs.jinv_g[7] = w * 2.0 * i10 * i11; cs.jinv_g[8] = w * i11 * i11;
-        cs.jfine[0] = J00; cs.jfine[1] = J10; cs.jfine[2] = J01; cs.jfine[3] = J11;
-        cs.absdet = fabs(det);
-      }
-      cs.status = st;
-    }
-    __syncthreads();
-    if (cs.status != MSFEM_CELL_CONVERGED) {
-      // malformed cell: report and move on (outputs NaN)
-      if (tid < 16) p.M[(int64_t)cell * 16 + tid] = __longlong_as_double(0x7ff8000000000000ll);
-      if (tid < 4) {
-        p.F[(int64_t)cell * 4 + tid] = __longlong_as_double(0x7ff8000000000000ll);
-        if (p.iters) p.iters[(int64_t)cell * 4 + tid] = 0;
-      }
-      if (tid == 0) {
-        p.status[cell] = cs.status;
-        if (p.rel_res) p.rel_res[cell] = __longlong_as_double(0x7ff8000000000000ll);
-        if (p.refinements) p.refinements[cell] = 0;
-      }
+    if (cell_begin<NMAX, NT>(p, cs, cell, N, c64, v64, d64, nullptr, tid) != MSFEM_CELL_CONVERGED) {
+      cell_report_bad(p, cs, cell, tid);
       __syncthreads();
       continue;
     }
-
-    // ---------------- assembly: 4-colour scatter -------------------------
-    {
-      const int nfc = N * N;
-      const double *tab = nullptr;
-      if (p.coef_kind == MSFEM_COEF_TABULATED)
-        tab = p.qp_values + (p.qp_offset ? p.qp_offset[cell] : (int64_t)cell * p.ncomp * 4 * nfc);
-      const double invN = 1.0 / (double)N;
-      const bool need_x = p.coef_kind != MSFEM_COEF_TABULATED && p.coef_kind != MSFEM_COEF_CONSTANT;
-      for (int col = 0; col < 4; ++col) {
-        const int ox = col & 1, oy = col >> 1;
-        const int nx = (N - ox + 1) >> 1, ny = (N - oy + 1) >> 1;
-        for (int idx = tid; idx < nx * ny; idx += NT) {
-          const int cx = ox + 2 * (idx % nx), cy = oy + 2 * (idx / nx);
-          const int fc = cx + N * cy;
-          double K[4][4];
-#pragma unroll
-          for (int i = 0; i < 4; ++i)
-#pragma unroll
-            for (int j = 0; j < 4; ++j) K[i][j] = 0.0;
-          double bload[4] = {0.0, 0.0, 0.0, 0.0};
-          bool bad = false;
-          double V[8];
-          if (!cs.affine) {
-            bilinear_map(cs.corners, cx * invN, cy * invN, V + 0);
-            bilinear_map(cs.corners, (cx + 1) * invN, cy * invN, V + 2);
-            bilinear_map(cs.corners, cx * invN, (cy + 1) * invN, V + 4);
-            bilinear_map(cs.corners, (cx + 1) * invN, (cy + 1) * invN, V + 6);
-          }
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const int qx = q & 1, qy = q >> 1;
-            const double xi = gauss2(qx), eta = gauss2(qy);
-            double xq[2] = {0.0, 0.0};
-            double Gm[3];
-            double A[3];
-            if (cs.affine) {
-              if (need_x) {
-                const double u = cx + xi, v = cy + eta;
-                xq[0] = cs.corners[0] + cs.jfine[0] * u + cs.jfine[2] * v;
-                xq[1] = cs.corners[1] + cs.jfine[1] * u + cs.jfine[3] * v;
-              }
-              coef_at<2>(p, xq, tab, q, nfc, fc, A);
-              Gm[0] = cs.jinv_g[0] * A[0] + cs.jinv_g[1] * A[1] + cs.jinv_g[2] * A[2];
-              Gm[1] = cs.jinv_g[3] * A[0] + cs.jinv_g[4] * A[1] + cs.jinv_g[5] * A[2];
-              Gm[2] = cs.jinv_g[6] * A[0] + cs.jinv_g[7] * A[1] + cs.jinv_g[8] * A[2];
-              const double wf = 0.25 * cs.absdet * p.f_value;
-#pragma unroll
-              for (int k = 0; k < 4; ++k) bload[k] += wf * lval(k & 1, qx) * lval(k >> 1, qy);
-            } else {
-              // J = sum_k V_k (x) grad psi_k(xi, eta)
-              double J00 = 0, J01 = 0, J10 = 0, J11 = 0;
-#pragma unroll
-              for (int k = 0; k < 4; ++k) {
-                const int kx = k & 1, ky = k >> 1;
-                const double gx = (kx ? 1.0 : -1.0) * lval(ky, qy);
-                const double gy = (ky ? 1.0 : -1.0) * lval(kx, qx);
-                const double psi = lval(kx, qx) * lval(ky, qy);
-                J00 += V[2 * k] * gx; J01 += V[2 * k] * gy;
-                J10 += V[2 * k + 1] * gx; J11 += V[2 * k + 1] * gy;
-                xq[0] += psi * V[2 * k]; xq[1] += psi * V[2 * k + 1];
-              }
-              const double det = J00 * J11 - J01 * J10;
-              if (!(det > 0.0)) bad = true;
-              const double id = 1.0 / det;
-              const double i00 = J11 * id, i01 = -J01 * id, i10 = -J10 * id, i11 = J00 * id;
-              const double w = 0.25 * fabs(det);
-              coef_at<2>(p, xq, tab, q, nfc, fc, A);
-              // T = Ji A, G = T Ji^T
-              const double t00 = i00 * A[0] + i01 * A[1], t01 = i00 * A[1] + i01 * A[2];
-              const double t10 = i10 * A[0] + i11 * A[1], t11 = i10 * A[1] + i11 * A[2];
-              Gm[0] = w * (t00 * i00 + t01 * i01);
-              Gm[1] = w * (t00 * i10 + t01 * i11);
-              Gm[2] = w * (t10 * i10 + t11 * i11);
-#pragma unroll
-              for (int k = 0; k < 4; ++k)
-                bload[k] += w * p.f_value * lval(k & 1, qx) * lval(k >> 1, qy);
-            }
-            // reference gradients at this Gauss point
-            double gx[4], gy[4], ax[4], ay[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-              const int kx = k & 1, ky = k >> 1;
-              gx[k] = (kx ? 1.0 : -1.0) * lval(ky, qy);
-              gy[k] = (ky ? 1.0 : -1.0) * lval(kx, qx);
-              ax[k] = Gm[0] * gx[k] + Gm[1] * gy[k];
-              ay[k] = Gm[1] * gx[k] + Gm[2] * gy[k];
-            }
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-#pragma unroll
-              for (int j = i; j < 4; ++j) K[i][j] = fma(gx[i], ax[j], fma(gy[i], ay[j], K[i][j]));
-          }
-          if (bad) cs.status = MSFEM_CELL_BAD_INPUT;
-          const int g0 = (cy + 1) * P + cx + 1;
-          const int g1 = g0 + 1, g2 = g0 + P, g3 = g0 + P + 1;
-          d64[g0] += K[0][0]; d64[g1] += K[1][1]; d64[g2] += K[2][2]; d64[g3] += K[3][3];
-          c64[4 * g0 + 0] += K[0][1];  // E  of node 0
-          c64[4 * g2 + 0] += K[2][3];  // E  of node 2
-          c64[4 * g0 + 2] += K[0][2];  // N  of node 0
-          c64[4 * g1 + 2] += K[1][3];  // N  of node 1
-          c64[4 * g0 + 1] += K[0][3];  // NE of node 0
-          c64[4 * g1 + 3] += K[1][2];  // NW of node 1
-          b64[g0] += bload[0]; b64[g1] += bload[1]; b64[g2] += bload[2]; b64[g3] += bload[3];
-        }
-        __syncthreads();
-      }
-    }
+    assemble2d<NT>(p, cs, cell, N, c64, d64, tid);
     if (cs.status != MSFEM_CELL_CONVERGED) {
-      if (tid < 16) p.M[(int64_t)cell * 16 + tid] = __longlong_as_double(0x7ff8000000000000ll);
-      if (tid < 4) {
-        p.F[(int64_t)cell * 4 + tid] = __longlong_as_double(0x7ff8000000000000ll);
-        if (p.iters) p.iters[(int64_t)cell * 4 + tid] = 0;
-      }
-      if (tid == 0) {
-        p.status[cell] = cs.status;
-        if (p.rel_res) p.rel_res[cell] = __longlong_as_double(0x7ff8000000000000ll);
-        if (p.refinements) p.refinements[cell] = 0;
-      }
+      cell_report_bad(p, cs, cell, tid);
       __syncthreads();
       continue;
     }
-
-    // ---------------- symmetric scaling ----------------------------------
-    for (int k = tid; k < n * n; k += NT) {
-      const int g = (k / n + 1) * P + k % n + 1;
-      const double d = d64[g];
-      const double s = rsqrt(d);
-      s64[g] = s;
-      b64[g] *= s;
-    }
-    __syncthreads();
-    double dmin_part = 1e300;
-    for (int k = tid; k < n * n; k += NT) {
-      const int ix = k % n, iy = k / n;
-      const int g = (iy + 1) * P + ix + 1;
-      const double s = s64[g];
-      double cc[4];
-      ld4(c64, g, cc);
-      cc[0] *= s * s64[g + 1];
-      cc[1] *= s * s64[g + P + 1];
-      cc[2] *= s * s64[g + P];
-      cc[3] *= s * s64[g + P - 1];
-      st4(c64, g, cc);
-      if (MIXED) {
-        float cf[4] = {(float)cc[0], (float)cc[1], (float)cc[2], (float)cc[3]};
-        st4(c32, g, cf);
-      }
-      const bool bnd = ix == 0 || iy == 0 || ix == N || iy == N;
-      const double d = d64[g];
-      if (bnd) {
-        // Dirichlet data phi~_i = D^1/2 g_i (BasisQ1 at the node)
-        double x[2], gv[4];
-        bilinear_map(cs.corners, ix / (double)N, iy / (double)N, x);
-        q1_eval<2>(cs.q1coef, cs.q1shift, cs.q1iscale, x, gv);
-        const double sq = d * s;
-        double t[4] = {gv[0] * sq, gv[1] * sq, gv[2] * sq, gv[3] * sq};
-        st4(v64, g, t);
-      } else {
-        dmin_part = fmin(dmin_part, d);
-        if (!(d > 0.0) || !isfinite(d)) cs.status = MSFEM_CELL_NAN;
-      }
-    }
-    // dmin (block min)
-#pragma unroll
-    for (int m = 16; m >= 1; m >>= 1) dmin_part = fmin(dmin_part, shfl_xor_d(dmin_part, m));
-    if (lane == 0) red[0][warp] = dmin_part;
-    __syncthreads();
-    if (tid == 0) {
-      double m = 1e300;
-      for (int w = 0; w < NW; ++w) m = fmin(m, red[0][w]);
-      cs.dmin = m;
-    }
+    scale2d<NT>(cs, N, c64, v64, d64, red[0], tid);
 
     // ---------------- right-hand sides ------------------------------------
     int gidx[NPT];
@@ -434,11 +620,16 @@ msfem2d_kernel(const KernelParams p) {
     warp_partials<4>(bbp, red[1], warp, lane);
     __syncthreads();
     if (warp == 0) {
-      const double t = warp0_finish<4>(red[1], NW, lane);
+      const double t = warp_finish<4>(red[1], NW, lane);
       if (lane < 4) cs.bb[lane] = t;
     }
     // warm start: x~0 = D^1/2 phi_warm on the interior, r0 = -(A~ phi~0)_I
     const bool warm = p.warm_basis != nullptr;
+    double xr[NPT][4], qr[NPT][4];
+#pragma unroll
+    for (int j = 0; j < NPT; ++j)
+#pragma unroll
+      for (int r = 0; r < 4; ++r) { xr[j][r] = 0.0; qr[j][r] = 0.0; }
     if (warm) {
       const double *wb = p.warm_basis + (p.basis_offset ? p.basis_offset[cell] : (int64_t)cell * 4 * n * n);
       __syncthreads();
@@ -447,11 +638,10 @@ msfem2d_kernel(const KernelParams p) {
         if (gidx[j] >= 0) {
           const int g = gidx[j];
           const int node = (g / P - 1) * n + (g % P - 1);
-          const double sq = d64[g] * s64[g];
-          double t[4];
+          const double sq = sqrt(dloc[j]);
 #pragma unroll
-          for (int r = 0; r < 4; ++r) t[r] = __ldg(wb + (int64_t)r * n * n + node) * sq;
-          st4(v64, g, t);
+          for (int r = 0; r < 4; ++r) xr[j][r] = __ldg(wb + (int64_t)r * n * n + node) * sq;
+          st4(v64, g, xr[j]);
         }
       __syncthreads();
 #pragma unroll
@@ -466,57 +656,142 @@ msfem2d_kernel(const KernelParams p) {
     __syncthreads();
 
     const double tol2 = p.tol * p.tol;
-    int total_iters[4] = {0, 0, 0, 0};
-
-    if (!MIXED) {
-      // ================= plain FP64 CG ====================================
-      double xr[NPT][4], qr[NPT][4];
+    // v64 becomes p~ (zero on the boundary ring)
+    for (int k = tid; k < 4 * N; k += NT) {
+      int ix, iy;
+      boundary_node(k, N, ix, iy);
+      const double z[4] = {0.0, 0.0, 0.0, 0.0};
+      st4(v64, (iy + 1) * P + ix + 1, z);
+    }
+    double rho_p[8];
 #pragma unroll
-      for (int j = 0; j < NPT; ++j)
+    for (int r = 0; r < 4; ++r) { rho_p[r] = 0.0; rho_p[4 + r] = 0.0; }
+#pragma unroll
+    for (int j = 0; j < NPT; ++j)
+      if (gidx[j] >= 0) {
+        st4(v64, gidx[j], rr[j]);
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
-          xr[j][r] = 0.0;
-          qr[j][r] = 0.0;
+          rho_p[r] = fma(rr[j][r], rr[j][r], rho_p[r]);
+          rho_p[4 + r] = fma(rr[j][r] * dloc[j], rr[j][r], rho_p[4 + r]);
         }
-      if (warm) {
-#pragma unroll
-        for (int j = 0; j < NPT; ++j)
-          if (gidx[j] >= 0) ld4(v64, gidx[j], xr[j]);
       }
-      // v64 becomes p~ (zero on the boundary ring)
-      for (int k = tid; k < 4 * N; k += NT) {
-        int ix, iy;
-        if (k < N) { ix = k; iy = 0; }
-        else if (k < 2 * N) { ix = N; iy = k - N; }
-        else if (k < 3 * N) { ix = N - (k - 2 * N); iy = N; }
-        else { ix = 0; iy = N - (k - 3 * N); }
-        const double z[4] = {0.0, 0.0, 0.0, 0.0};
-        st4(v64, (iy + 1) * P + ix + 1, z);
+    warp_partials<8>(rho_p, red[0], warp, lane);
+    __syncthreads();
+    if (warp == 0) {
+      const double t = warp_finish<8>(red[0], NW, lane);
+      const double nu = shfl_xor_d(t, 4);  // lane r (<4) gets value 4+r
+      if (lane < 4) {
+        cs.rho[lane] = t;
+        const bool conv = nu <= tol2 * cs.bb[lane];
+        cs.active[lane] = !conv;
+        cs.iters[lane] = 0;
+        cs.beta[lane] = 0.0;
       }
-      double rho_p[8];
-#pragma unroll
-      for (int r = 0; r < 4; ++r) { rho_p[r] = 0.0; rho_p[4 + r] = 0.0; }
+      __syncwarp();
+      if (lane == 0) {
+        int any = 0, nn2 = 0;
+        for (int r = 0; r < 4; ++r) {
+          any |= cs.active[r];
+          if (cs.active[r] && cs.dmin * cs.rho[r] <= 100.0 * tol2 * cs.bb[r]) nn2 = 1;
+        }
+        cs.done = !any;
+        cs.need_nu = nn2 || p.check_interval == 1;
+      }
+    }
+    __syncthreads();
+    int it = 0;
+    while (!cs.done) {
+      ++it;
+      // q = A~ p, sigma = p.q
+      double sg[4] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll
       for (int j = 0; j < NPT; ++j)
         if (gidx[j] >= 0) {
-          st4(v64, gidx[j], rr[j]);
+          double pj[4];
+          stencil9<double>(c64, v64, gidx[j], P, qr[j]);
+          ld4(v64, gidx[j], pj);
 #pragma unroll
-          for (int r = 0; r < 4; ++r) {
-            rho_p[r] = fma(rr[j][r], rr[j][r], rho_p[r]);
-            rho_p[4 + r] = fma(rr[j][r] * dloc[j], rr[j][r], rho_p[4 + r]);
-          }
+          for (int r = 0; r < 4; ++r) sg[r] = fma(pj[r], qr[j][r], sg[r]);
         }
-      warp_partials<8>(rho_p, red[0], warp, lane);
+      warp_partials<4>(sg, red[1], warp, lane);
       __syncthreads();
       if (warp == 0) {
-        const double t = warp0_finish<8>(red[0], NW, lane);
-        const double nu = shfl_xor_d(t, 4);  // lane r (<4) gets value 4+r
+        const double t = warp_finish<4>(red[1], NW, lane);
         if (lane < 4) {
-          cs.rho[lane] = t;
-          const bool conv = nu <= tol2 * cs.bb[lane];
-          cs.active[lane] = !conv;
-          cs.iters[lane] = 0;
-          cs.beta[lane] = 0.0;
+          double a = 0.0;
+          if (cs.active[lane]) {
+            if (cs.rho[lane] == 0.0) {
+              // exact solution reached in the previous step
+              cs.active[lane] = 0;
+              cs.iters[lane] = it - 1;
+            } else {
+              a = cs.rho[lane] / t;
+              if (!isfinite(a) || !(t > 0.0)) {
+                a = 0.0;
+                cs.active[lane] = 0;
+                cs.iters[lane] = -it;  // breakdown marker
+              }
+            }
+          }
+          cs.alpha[lane] = a;
+        }
+      }
+      __syncthreads();
+      const bool need_nu = cs.need_nu;
+      const double al[4] = {cs.alpha[0], cs.alpha[1], cs.alpha[2], cs.alpha[3]};
+      double rp[8];
+#pragma unroll
+      for (int r = 0; r < 8; ++r) rp[r] = 0.0;
+#pragma unroll
+      for (int j = 0; j < NPT; ++j)
+        if (gidx[j] >= 0) {
+          double pj[4];
+          ld4(v64, gidx[j], pj);
+#pragma unroll
+          for (int r = 0; r < 4; ++r) {
+            xr[j][r] = fma(al[r], pj[r], xr[j][r]);
+            rr[j][r] = fma(-al[r], qr[j][r], rr[j][r]);
+            rp[r] = fma(rr[j][r], rr[j][r], rp[r]);
+          }
+          if (need_nu) {
+#pragma unroll
+            for (int r = 0; r < 4; ++r) rp[4 + r] = fma(rr[j][r] * dloc[j], rr[j][r], rp[4 + r]);
+          }
+        }
+      if (need_nu) {
+        warp_partials<8>(rp, red[0], warp, lane);
+      } else {
+        double r4[4] = {rp[0], rp[1], rp[2], rp[3]};
+        warp_partials<4>(r4, red[0], warp, lane);
+      }
+      __syncthreads();
+      if (warp == 0) {
+        double t, nu = 0.0;
+        if (need_nu) {
+          t = warp_finish<8>(red[0], NW, lane);
+          nu = shfl_xor_d(t, 4);
+        } else {
+          t = warp_finish<4>(red[0], NW, lane);
+        }
+        if (lane < 4) {
+          double b = 0.0;
+          if (cs.active[lane]) {
+            if (!isfinite(t)) {
+              cs.active[lane] = 0;
+              cs.iters[lane] = -it;
+            } else if (t == 0.0 || (need_nu && nu <= tol2 * cs.bb[lane])) {
+              cs.active[lane] = 0;
+              cs.iters[lane] = it;
+            } else if (it >= p.maxit) {
+              cs.active[lane] = 0;
+              cs.iters[lane] = -1000000 - it;  // maxit marker
+            } else {
+              b = t / cs.rho[lane];
+              cs.rho[lane] = t;
+            }
+          }
+          cs.beta[lane] = b;
         }
         __syncwarp();
         if (lane == 0) {
@@ -526,398 +801,415 @@ msfem2d_kernel(const KernelParams p) {
             if (cs.active[r] && cs.dmin * cs.rho[r] <= 100.0 * tol2 * cs.bb[r]) nn2 = 1;
           }
           cs.done = !any;
-          cs.need_nu = nn2 || p.check_interval == 1;
+          cs.need_nu = nn2 || (p.check_interval > 0 && ((it + 1) % p.check_interval) == 0);
         }
       }
       __syncthreads();
-      int it = 0;
-      while (!cs.done) {
-        ++it;
-        // q = A~ p, sigma = p.q
-        double sg[4] = {0.0, 0.0, 0.0, 0.0};
-#pragma unroll
-        for (int j = 0; j < NPT; ++j)
-          if (gidx[j] >= 0) {
-            double pj[4];
-            stencil9<double>(c64, v64, gidx[j], P, qr[j]);
-            ld4(v64, gidx[j], pj);
-#pragma unroll
-            for (int r = 0; r < 4; ++r) sg[r] = fma(pj[r], qr[j][r], sg[r]);
-          }
-        warp_partials<4>(sg, red[1], warp, lane);
-        __syncthreads();
-        if (warp == 0) {
-          const double t = warp0_finish<4>(red[1], NW, lane);
-          if (lane < 4) {
-            double a = 0.0;
-            if (cs.active[lane]) {
-              if (cs.rho[lane] == 0.0) {
-                // exact solution reached in the previous step
-                cs.active[lane] = 0;
-                cs.iters[lane] = it - 1;
-              } else {
-                a = cs.rho[lane] / t;
-                if (!isfinite(a) || !(t > 0.0)) {
-                  a = 0.0;
-                  cs.active[lane] = 0;
-                  cs.iters[lane] = -it;  // breakdown marker
-                }
-              }
-            }
-            cs.alpha[lane] = a;
-          }
-        }
-        __syncthreads();
-        const bool need_nu = cs.need_nu;
-        double al[4] = {cs.alpha[0], cs.alpha[1], cs.alpha[2], cs.alpha[3]};
-        double rp[8];
-#pragma unroll
-        for (int r = 0; r < 8; ++r) rp[r] = 0.0;
-#pragma unroll
-        for (int j = 0; j < NPT; ++j)
-          if (gidx[j] >= 0) {
-            double pj[4];
-            ld4(v64, gidx[j], pj);
-#pragma unroll
-            for (int r = 0; r < 4; ++r) {
-              xr[j][r] = fma(al[r], pj[r], xr[j][r]);
-              rr[j][r] = fma(-al[r], qr[j][r], rr[j][r]);
-              rp[r] = fma(rr[j][r], rr[j][r], rp[r]);
-            }
-            if (need_nu) {
-#pragma unroll
-              for (int r = 0; r < 4; ++r) rp[4 + r] = fma(rr[j][r] * dloc[j], rr[j][r], rp[4 + r]);
-            }
-          }
-        if (need_nu) {
-          warp_partials<8>(rp, red[0], warp, lane);
-        } else {
-          double r4[4] = {rp[0], rp[1], rp[2], rp[3]};
-          warp_partials<4>(r4, red[0], warp, lane);
-        }
-        __syncthreads();
-        if (warp == 0) {
-          double t, nu = 0.0;
-          if (need_nu) {
-            t = warp0_finish<8>(red[0], NW, lane);
-            nu = shfl_xor_d(t, 4);
-          } else {
-            t = warp0_finish<4>(red[0], NW, lane);
-          }
-          if (lane < 4) {
-            double b = 0.0;
-            if (cs.active[lane]) {
-              if (!isfinite(t)) {
-                cs.active[lane] = 0;
-                cs.iters[lane] = -it;
-              } else if (t == 0.0 || (need_nu && nu <= tol2 * cs.bb[lane])) {
-                cs.active[lane] = 0;
-                cs.iters[lane] = it;
-              } else if (it >= p.maxit) {
-                cs.active[lane] = 0;
-                cs.iters[lane] = -1000000 - it;  // maxit marker
-              } else {
-                b = t / cs.rho[lane];
-                cs.rho[lane] = t;
-              }
-            }
-            cs.beta[lane] = b;
-          }
-          __syncwarp();
-          if (lane == 0) {
-            int any = 0, nn2 = 0;
-            for (int r = 0; r < 4; ++r) {
-              any |= cs.active[r];
-              if (cs.active[r] && cs.dmin * cs.rho[r] <= 100.0 * tol2 * cs.bb[r]) nn2 = 1;
-            }
-            cs.done = !any;
-            cs.need_nu = nn2 || (p.check_interval > 0 && ((it + 1) % p.check_interval) == 0);
-          }
-        }
-        __syncthreads();
-        if (cs.done) break;
-        const double be[4] = {cs.beta[0], cs.beta[1], cs.beta[2], cs.beta[3]};
-#pragma unroll
-        for (int j = 0; j < NPT; ++j)
-          if (gidx[j] >= 0) {
-            double pj[4];
-            ld4(v64, gidx[j], pj);
-#pragma unroll
-            for (int r = 0; r < 4; ++r) pj[r] = fma(be[r], pj[r], rr[j][r]);
-            st4(v64, gidx[j], pj);
-          }
-        __syncthreads();
-      }
-      // phi~ = [x~ ; D^1/2 g] into v64
+      if (cs.done) break;
+      const double be[4] = {cs.beta[0], cs.beta[1], cs.beta[2], cs.beta[3]};
 #pragma unroll
       for (int j = 0; j < NPT; ++j)
-        if (gidx[j] >= 0) st4(v64, gidx[j], xr[j]);
-      for (int k = tid; k < 4 * N; k += NT) {
-        int ix, iy;
-        if (k < N) { ix = k; iy = 0; }
-        else if (k < 2 * N) { ix = N; iy = k - N; }
-        else if (k < 3 * N) { ix = N - (k - 2 * N); iy = N; }
-        else { ix = 0; iy = N - (k - 3 * N); }
-        const int g = (iy + 1) * P + ix + 1;
-        double x[2], gv[4];
-        bilinear_map(cs.corners, ix / (double)N, iy / (double)N, x);
-        q1_eval<2>(cs.q1coef, cs.q1shift, cs.q1iscale, x, gv);
-        const double sq = d64[g] * s64[g];
-        double t[4] = {gv[0] * sq, gv[1] * sq, gv[2] * sq, gv[3] * sq};
-        st4(v64, g, t);
-      }
-      __syncthreads();
-      if (tid == 0) cs.refinements = 0;
-    } else {
-      // ================= MIXED: FP32 inner CG + FP64 refinement ===========
-      // x~ lives in v64 (interior); r (FP64) in rr.  v32 holds p~ (FP32),
-      // zero on the boundary ring.
-      if (tid == 0) cs.refinements = 0;
-      int ref = 0;
-      for (;;) {
-        // true residual norm and convergence test (FP64)
-        double nup[4] = {0.0, 0.0, 0.0, 0.0};
+        if (gidx[j] >= 0) {
+          double pj[4];
+          ld4(v64, gidx[j], pj);
 #pragma unroll
-        for (int j = 0; j < NPT; ++j)
-          if (gidx[j] >= 0)
-#pragma unroll
-            for (int r = 0; r < 4; ++r) nup[r] = fma(rr[j][r] * dloc[j], rr[j][r], nup[r]);
-        warp_partials<4>(nup, red[0], warp, lane);
-        __syncthreads();
-        if (warp == 0) {
-          const double t = warp0_finish<4>(red[0], NW, lane);
-          if (lane < 4) {
-            if (!isfinite(t)) {
-              cs.active[lane] = 0;
-              cs.iters[lane] = -1;
-            } else {
-              cs.active[lane] = !(t <= tol2 * cs.bb[lane]);
-            }
-          }
-          __syncwarp();
-          if (lane == 0) {
-            int any = 0;
-            for (int r = 0; r < 4; ++r) any |= cs.active[r];
-            if (any && ref >= p.max_refine) {
-              for (int r = 0; r < 4; ++r)
-                if (cs.active[r]) { cs.active[r] = 0; cs.iters[r] = -1000000; }
-              any = 0;
-            }
-            cs.done = !any;
-          }
+          for (int r = 0; r < 4; ++r) pj[r] = fma(be[r], pj[r], rr[j][r]);
+          st4(v64, gidx[j], pj);
         }
-        __syncthreads();
-        if (cs.done) break;
-        ++ref;
-        // ---- inner FP32 CG on A~ d = r (active RHS only)
-        float act[4];
-#pragma unroll
-        for (int r = 0; r < 4; ++r) act[r] = cs.active[r] ? 1.0f : 0.0f;
-        float r32[NPT][4], d32[NPT][4], q32[NPT][4];
-        float rho32[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-        for (int j = 0; j < NPT; ++j) {
-#pragma unroll
-          for (int r = 0; r < 4; ++r) {
-            r32[j][r] = (float)rr[j][r] * act[r];
-            d32[j][r] = 0.0f;
-            q32[j][r] = 0.0f;
-          }
-          if (gidx[j] >= 0) {
-            st4(v32, gidx[j], r32[j]);
-#pragma unroll
-            for (int r = 0; r < 4; ++r) rho32[r] = fmaf(r32[j][r], r32[j][r], rho32[r]);
-          }
-        }
-        // block reduce rho32 (all threads compute the totals redundantly)
-        int buf = 0;
-        {
-          float tmp[4] = {rho32[0], rho32[1], rho32[2], rho32[3]};
-          const float tot = warp_transpose_reduce<4>(tmp, lane);
-          if ((lane & 7) == 0) red32[buf][warp * 4 + (lane >> 3)] = tot;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-          float s = 0.f;
-          for (int w = 0; w < NW; ++w) s += red32[buf][w * 4 + r];
-          rho32[r] = s;
-        }
-        buf ^= 1;
-        const float itol2 = p.inner_tol * p.inner_tol;
-        float rho0[4] = {rho32[0], rho32[1], rho32[2], rho32[3]};
-        bool inner_act[4];
-#pragma unroll
-        for (int r = 0; r < 4; ++r) inner_act[r] = act[r] > 0.0f && rho32[r] > 0.0f;
-        int iit = 0;
-        for (;;) {
-          bool any = inner_act[0] || inner_act[1] || inner_act[2] || inner_act[3];
-          if (!any || iit >= p.inner_maxit) break;
-          ++iit;
-          // q = A~ p, sigma
-          float sg[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-          for (int j = 0; j < NPT; ++j)
-            if (gidx[j] >= 0) {
-              float pj[4];
-              stencil9<float>(c32, v32, gidx[j], P, q32[j]);
-              ld4(v32, gidx[j], pj);
-#pragma unroll
-              for (int r = 0; r < 4; ++r) sg[r] = fmaf(pj[r], q32[j][r], sg[r]);
-            }
-          {
-            const float tot = warp_transpose_reduce<4>(sg, lane);
-            if ((lane & 7) == 0) red32[buf][warp * 4 + (lane >> 3)] = tot;
-          }
-          __syncthreads();
-          float al[4];
-#pragma unroll
-          for (int r = 0; r < 4; ++r) {
-            float s = 0.f;
-            for (int w = 0; w < NW; ++w) s += red32[buf][w * 4 + r];
-            al[r] = (inner_act[r] && s > 0.f) ? rho32[r] / s : 0.0f;
-          }
-          buf ^= 1;
-          float rp[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-          for (int j = 0; j < NPT; ++j)
-            if (gidx[j] >= 0) {
-              float pj[4];
-              ld4(v32, gidx[j], pj);
-#pragma unroll
-              for (int r = 0; r < 4; ++r) {
-                d32[j][r] = fmaf(al[r], pj[r], d32[j][r]);
-                r32[j][r] = fmaf(-al[r], q32[j][r], r32[j][r]);
-                rp[r] = fmaf(r32[j][r], r32[j][r], rp[r]);
-              }
-            }
-          {
-            const float tot = warp_transpose_reduce<4>(rp, lane);
-            if ((lane & 7) == 0) red32[buf][warp * 4 + (lane >> 3)] = tot;
-          }
-          __syncthreads();
-          float be[4];
-#pragma unroll
-          for (int r = 0; r < 4; ++r) {
-            float s = 0.f;
-            for (int w = 0; w < NW; ++w) s += red32[buf][w * 4 + r];
-            be[r] = 0.0f;
-            if (inner_act[r]) {
-              if (!(s <= itol2 * rho0[r]) && isfinite(s)) {
-                be[r] = s / rho32[r];
-                rho32[r] = s;
-              } else {
-                inner_act[r] = false;
-              }
-              total_iters[r] += 1;
-            }
-          }
-          buf ^= 1;
-#pragma unroll
-          for (int j = 0; j < NPT; ++j)
-            if (gidx[j] >= 0) {
-              float pj[4];
-              ld4(v32, gidx[j], pj);
-#pragma unroll
-              for (int r = 0; r < 4; ++r) pj[r] = fmaf(be[r], pj[r], r32[j][r]);
-              st4(v32, gidx[j], pj);
-            }
-          __syncthreads();
-        }
-        // ---- x~ += d (FP64), new FP64 residual r = -(A~ phi~)_I
-#pragma unroll
-        for (int j = 0; j < NPT; ++j)
-          if (gidx[j] >= 0) {
-            double xj[4];
-            ld4(v64, gidx[j], xj);
-#pragma unroll
-            for (int r = 0; r < 4; ++r) xj[r] += (double)d32[j][r];
-            st4(v64, gidx[j], xj);
-          }
-        __syncthreads();
-#pragma unroll
-        for (int j = 0; j < NPT; ++j)
-          if (gidx[j] >= 0) {
-            double y[4];
-            stencil9<double>(c64, v64, gidx[j], P, y);
-#pragma unroll
-            for (int r = 0; r < 4; ++r) rr[j][r] = -y[r];
-          }
-      }
-      if (tid == 0) cs.refinements = ref;
       __syncthreads();
     }
+    // phi~ = [x~ ; D^1/2 g] into v64
+#pragma unroll
+    for (int j = 0; j < NPT; ++j)
+      if (gidx[j] >= 0) st4(v64, gidx[j], xr[j]);
+    for (int k = tid; k < 4 * N; k += NT) {
+      int ix, iy;
+      boundary_node(k, N, ix, iy);
+      double t[4];
+      boundary_value(cs, d64, N, P, ix, iy, t);
+      st4(v64, (iy + 1) * P + ix + 1, t);
+    }
+    __syncthreads();
 
     // ---------------- epilogue: M, F, true residual ----------------------
-    {
-      double acc[32];
+    double acc[32];
 #pragma unroll
-      for (int i = 0; i < 32; ++i) acc[i] = 0.0;
-      for (int k = tid; k < n * n; k += NT) {
-        const int ix = k % n, iy = k / n;
-        const int g = (iy + 1) * P + ix + 1;
-        double y[4], ph[4];
-        stencil9<double>(c64, v64, g, P, y);
-        ld4(v64, g, ph);
-        const double bl = b64[g];
+    for (int i = 0; i < 32; ++i) acc[i] = 0.0;
+    for (int k = tid; k < n * n; k += NT) {
+      const int ix = k % n, iy = k / n;
+      const int g = (iy + 1) * P + ix + 1;
+      double y[4], ph[4];
+      stencil9<double>(c64, v64, g, P, y);
+      ld4(v64, g, ph);
+      epilogue_node(p, cs, d64, N, P, ix, iy, ph, y, acc);
+      if (ix > 0 && iy > 0 && ix < N && iy < N) {
+        const double d = d64[g];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
+        for (int j = 0; j < 4; ++j) acc[20 + j] = fma(y[j] * d, y[j], acc[20 + j]);
+      }
+    }
+    write_basis<NT>(p, cell, N, v64, d64, tid);
+    epilogue_finish<NT, false>(p, cs, cell, acc, redE, false, zero_iters, tid);
+  }
+}
+
+// ===========================================================================
+// Mixed form: FP64 residual refinement around an FP32 CG.  Thread t owns
+// interior column ix = 1 + t % (N-1) and rows s0 .. s0+S-1 of it,
+// s0 = 1 + S (t / (N-1)): the strip's own search-direction values stay in
+// registers, only its two neighbour columns and two halo rows come from
+// shared memory.
+// ===========================================================================
+template <int NMAX, int NT, int S, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
+msfem2d_mixed_kernel(const KernelParams p) {
+  using L = Smem2D<NMAX>;
+  constexpr int NW = NT / 32;
+  static_assert((NMAX - 1) * ((NMAX - 1 + S - 1) / S) <= NT, "strips must cover the interior");
+  static_assert(NW * 32 * sizeof(double) <= 16 * L::G, "epilogue partials fit in v32");
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double *c64 = reinterpret_cast<double *>(smem_raw + L::kC64);
+  double *v64 = reinterpret_cast<double *>(smem_raw + L::kV64);
+  double *d64 = reinterpret_cast<double *>(smem_raw + L::kD64);
+  float *v32 = reinterpret_cast<float *>(smem_raw + L::kV32);
+  __shared__ CellShared2D cs;
+  __shared__ double red[2][NW * 8];
+  __shared__ float red32[2][NW * 4];
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+  for (;;) {
+    if (tid == 0) {
+      const unsigned wi = atomicAdd(p.queue, 1u);
+      cs.cell = wi < (unsigned)p.n_cells ? (p.order ? p.order[wi] : (int)wi) : -1;
+    }
+    __syncthreads();
+    const int cell = cs.cell;
+    if (cell < 0) break;
+    const int N = p.n_fine ? p.n_fine[cell] : p.n_fine_uniform;
+    const int P = N + 3, n = N + 1;
+
+    if (cell_begin<NMAX, NT>(p, cs, cell, N, c64, v64, d64, v32, tid) != MSFEM_CELL_CONVERGED) {
+      cell_report_bad(p, cs, cell, tid);
+      __syncthreads();
+      continue;
+    }
+    assemble2d<NT>(p, cs, cell, N, c64, d64, tid);
+    if (cs.status != MSFEM_CELL_CONVERGED) {
+      cell_report_bad(p, cs, cell, tid);
+      __syncthreads();
+      continue;
+    }
+    scale2d<NT>(cs, N, c64, v64, d64, red[0], tid);
+
+    // strip of this thread
+    const int ncol = N - 1;
+    const int nstrip = ncol > 0 ? (ncol + S - 1) / S : 0;
+    const bool own = tid < ncol * nstrip;
+    const int ix = own ? 1 + tid % ncol : 1;
+    const int s0 = own ? 1 + S * (tid / ncol) : 1;
+    const int ns = own ? min(S, N - s0) : 0;
+    const int g0 = (s0 + 1) * P + ix + 1;
+
+    // FP64 right-hand sides (and warm start)
+    double r64[S][4];
+    double bbp[4] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll
-          for (int j = 0; j < 4; ++j) acc[4 * i + j] = fma(ph[i], y[j], acc[4 * i + j]);
-          acc[16 + i] = fma(ph[i], bl, acc[16 + i]);
-        }
-        if (ix > 0 && iy > 0 && ix < N && iy < N) {
-          const double d = d64[g];
+    for (int s = 0; s < S; ++s) {
 #pragma unroll
-          for (int j = 0; j < 4; ++j) acc[20 + j] = fma(y[j] * d, y[j], acc[20 + j]);
-        }
-        if (p.basis) {
-          const double s = s64[g];
-          double *out = p.basis + (p.basis_offset ? p.basis_offset[cell] : (int64_t)cell * 4 * n * n);
+      for (int r = 0; r < 4; ++r) r64[s][r] = 0.0;
+      if (s < ns) {
+        double y[4];
+        stencil9<double>(c64, v64, g0 + s * P, P, y);
+        const double d = d64[g0 + s * P];
 #pragma unroll
-          for (int i = 0; i < 4; ++i) out[(int64_t)i * n * n + k] = ph[i] * s;
+        for (int r = 0; r < 4; ++r) {
+          r64[s][r] = -y[r];
+          bbp[r] = fma(r64[s][r] * d, r64[s][r], bbp[r]);
         }
       }
-      const double tot = warp_transpose_reduce<32>(acc, lane);
-      red[0][warp * 32 + lane] = tot;
+    }
+    warp_partials<4>(bbp, red[1], warp, lane);
+    __syncthreads();
+    if (warp == 0) {
+      const double t = warp_finish<4>(red[1], NW, lane);
+      if (lane < 4) cs.bb[lane] = t;
+    }
+    if (p.warm_basis != nullptr) {
+      const double *wb = p.warm_basis + (p.basis_offset ? p.basis_offset[cell] : (int64_t)cell * 4 * n * n);
+      __syncthreads();
+#pragma unroll
+      for (int s = 0; s < S; ++s)
+        if (s < ns) {
+          const int g = g0 + s * P;
+          const int node = (s0 + s) * n + ix;
+          const double sq = sqrt(d64[g]);
+          double t[4];
+#pragma unroll
+          for (int r = 0; r < 4; ++r) t[r] = __ldg(wb + (int64_t)r * n * n + node) * sq;
+          st4(v64, g, t);
+        }
+      __syncthreads();
+#pragma unroll
+      for (int s = 0; s < S; ++s)
+        if (s < ns) {
+          double y[4];
+          stencil9<double>(c64, v64, g0 + s * P, P, y);
+#pragma unroll
+          for (int r = 0; r < 4; ++r) r64[s][r] = -y[r];
+        }
+    }
+    // FP32 couplings of the strip: E, W, N, S, NE, SW, NW, SE of every row
+    float cE[S], cW[S], cN[S], cS[S], cNE[S], cSW[S], cNW[S], cSE[S];
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+      const int g = g0 + s * P;
+      const bool v = s < ns;
+      cE[s] = v ? (float)c64[4 * g + 0] : 0.f;
+      cNE[s] = v ? (float)c64[4 * g + 1] : 0.f;
+      cN[s] = v ? (float)c64[4 * g + 2] : 0.f;
+      cNW[s] = v ? (float)c64[4 * g + 3] : 0.f;
+      cW[s] = v ? (float)c64[4 * (g - 1) + 0] : 0.f;
+      cS[s] = v ? (float)c64[4 * (g - P) + 2] : 0.f;
+      cSW[s] = v ? (float)c64[4 * (g - P - 1) + 1] : 0.f;
+      cSE[s] = v ? (float)c64[4 * (g - P + 1) + 3] : 0.f;
+    }
+
+    const double tol2 = p.tol * p.tol;
+    const float itol2 = p.inner_tol * p.inner_tol;
+    int total_iters[4] = {0, 0, 0, 0};
+    int ref = 0;
+    int buf = 0;
+    // lane-parallel 4-value block sum (every warp ends with the totals)
+    auto block_sum4 = [&](float (&v)[4]) {
+      const float t = warp_transpose_reduce<4>(v, lane);
+      if ((lane & 7) == 0) red32[buf][warp * 4 + (lane >> 3)] = t;
+      __syncthreads();
+      float s = 0.f;
+      for (int i = lane; i < NW * 4; i += 32) s += red32[buf][i];
+#pragma unroll
+      for (int m = 4; m < 32; m <<= 1) s += shfl_xor_d(s, m);
+#pragma unroll
+      for (int r = 0; r < 4; ++r) v[r] = __shfl_sync(0xffffffffu, s, r);
+      buf ^= 1;
+    };
+    for (;;) {
+      // ---- true FP64 residual norm and convergence test
+      double nup[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+      for (int s = 0; s < S; ++s)
+        if (s < ns) {
+          const double d = d64[g0 + s * P];
+#pragma unroll
+          for (int r = 0; r < 4; ++r) nup[r] = fma(r64[s][r] * d, r64[s][r], nup[r]);
+        }
+      warp_partials<4>(nup, red[0], warp, lane);
       __syncthreads();
       if (warp == 0) {
-        double s = 0.0;
-        for (int w = 0; w < NW; ++w) s += red[0][w * 32 + lane];
-        // lane v holds value v
-        if (lane < 16) p.M[(int64_t)cell * 16 + lane] = s;
-        else if (lane < 20) p.F[(int64_t)cell * 4 + (lane - 16)] = s;
-        double rel = 0.0;
-        if (lane >= 20 && lane < 24) {
-          const double bb = cs.bb[lane - 20];
-          rel = bb > 0.0 ? sqrt(s / bb) : sqrt(s);
-        }
-#pragma unroll
-        for (int m = 16; m >= 1; m >>= 1) rel = fmax(rel, shfl_xor_d(rel, m));
+        const double t = warp_finish<4>(red[0], NW, lane);
         if (lane < 4) {
-          int itv = cs.iters[lane];
-          if (MIXED) {
-            // iters holds -1 / -1000000 markers only; count inner iterations
-            if (p.iters) p.iters[(int64_t)cell * 4 + lane] = total_iters[lane];
-          } else if (p.iters) {
-            p.iters[(int64_t)cell * 4 + lane] = itv >= 0 ? itv : (itv <= -1000000 ? -itv - 1000000 : -itv);
+          cs.nu[lane] = t;
+          if (!isfinite(t)) {
+            cs.active[lane] = 0;
+            cs.iters[lane] = -1;
+          } else {
+            cs.active[lane] = !(t <= tol2 * cs.bb[lane]);
           }
         }
+        __syncwarp();
         if (lane == 0) {
-          int st = cs.status;  // MSFEM_CELL_NAN when a diagonal was not positive
-          for (int r = 0; r < 4; ++r) {
-            const int itv = cs.iters[r];
-            if (itv <= -1000000) st = st == MSFEM_CELL_CONVERGED ? MSFEM_CELL_MAXIT : st;
-            else if (itv < 0) st = MSFEM_CELL_NAN;
+          int any = 0;
+          for (int r = 0; r < 4; ++r) any |= cs.active[r];
+          if (any && ref >= p.max_refine) {
+            for (int r = 0; r < 4; ++r)
+              if (cs.active[r]) { cs.active[r] = 0; cs.iters[r] = -1000000; }
+            any = 0;
           }
-          if (!isfinite(rel)) st = MSFEM_CELL_NAN;
-          p.status[cell] = st;
-          if (p.rel_res) p.rel_res[cell] = rel;
-          if (p.refinements) p.refinements[cell] = cs.refinements;
+          cs.done = !any;
         }
       }
       __syncthreads();
+      if (cs.done) break;
+      ++ref;
+      // ---- inner FP32 CG on A~ d = r (active RHS only)
+      float act[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) act[r] = cs.active[r] ? 1.0f : 0.0f;
+      float rv[S][4], pv[S][4], qv[S][4], dv[S][4];
+      float rho[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          rv[s][r] = s < ns ? (float)r64[s][r] * act[r] : 0.0f;
+          pv[s][r] = rv[s][r];
+          dv[s][r] = 0.0f;
+          qv[s][r] = 0.0f;
+          rho[r] = fmaf(rv[s][r], rv[s][r], rho[r]);
+        }
+        if (s < ns) st4(v32, g0 + s * P, pv[s]);
+      }
+      block_sum4(rho);
+      const float rho0[4] = {rho[0], rho[1], rho[2], rho[3]};
+      bool iact[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) iact[r] = act[r] > 0.0f && rho[r] > 0.0f;
+      int iit = 0;
+      for (;;) {
+        if (!(iact[0] || iact[1] || iact[2] || iact[3]) || iit >= p.inner_maxit) break;
+        ++iit;
+        // q = A~ p on the strip.  Own-column neighbours come from registers
+        // (halo rows from shared memory); each value of the two neighbour
+        // columns is loaded once and scattered into the (up to three) rows
+        // that couple to it.
+        float sg[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int s = 0; s < S; ++s)
+#pragma unroll
+          for (int r = 0; r < 4; ++r) qv[s][r] = pv[s][r];
+        if (ns > 0) {
+          float t4[4];
+          ld4(v32, g0 - P, t4);  // row below the strip
+#pragma unroll
+          for (int r = 0; r < 4; ++r) qv[0][r] = fmaf(cS[0], t4[r], qv[0][r]);
+#pragma unroll
+          for (int s = 0; s < S; ++s) {
+            if (s < ns) {
+              if (s > 0) {
+#pragma unroll
+                for (int r = 0; r < 4; ++r) qv[s][r] = fmaf(cS[s], pv[s - 1][r], qv[s][r]);
+              }
+              if (s + 1 < ns) {
+#pragma unroll
+                for (int r = 0; r < 4; ++r) qv[s][r] = fmaf(cN[s], pv[s + 1][r], qv[s][r]);
+              } else {
+                ld4(v32, g0 + (s + 1) * P, t4);  // row above the strip
+#pragma unroll
+                for (int r = 0; r < 4; ++r) qv[s][r] = fmaf(cN[s], t4[r], qv[s][r]);
+              }
+            }
+          }
+#pragma unroll
+          for (int t = -1; t <= S; ++t) {
+            if (t <= ns) {
+              ld4(v32, g0 + t * P - 1, t4);  // left column, row s0 + t
+              if (t >= 1 && t - 1 < ns) {
+#pragma unroll
+                for (int r = 0; r < 4; ++r) qv[t - 1][r] = fmaf(cNW[t - 1], t4[r], qv[t - 1][r]);
+              }
+              if (t >= 0 && t < ns) {
+#pragma unroll
+                for (int r = 0; r < 4; ++r) qv[t][r] = fmaf(cW[t], t4[r], qv[t][r]);
+              }
+              if (t + 1 < ns && t + 1 < S) {
+#pragma unroll
+                for (int r = 0; r < 4; ++r) qv[t + 1][r] = fmaf(cSW[t + 1], t4[r], qv[t + 1][r]);
+              }
+              ld4(v32, g0 + t * P + 1, t4);  // right column, row s0 + t
+              if (t >= 1 && t - 1 < ns) {
+#pragma unroll
+                for (int r = 0; r < 4; ++r) qv[t - 1][r] = fmaf(cNE[t - 1], t4[r], qv[t - 1][r]);
+              }
+              if (t >= 0 && t < ns) {
+#pragma unroll
+                for (int r = 0; r < 4; ++r) qv[t][r] = fmaf(cE[t], t4[r], qv[t][r]);
+              }
+              if (t + 1 < ns && t + 1 < S) {
+#pragma unroll
+                for (int r = 0; r < 4; ++r) qv[t + 1][r] = fmaf(cSE[t + 1], t4[r], qv[t + 1][r]);
+              }
+            }
+          }
+#pragma unroll
+          for (int s = 0; s < S; ++s)
+#pragma unroll
+            for (int r = 0; r < 4; ++r) sg[r] = fmaf(pv[s][r], qv[s][r], sg[r]);
+        }
+        block_sum4(sg);
+        float al[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) al[r] = (iact[r] && sg[r] > 0.f) ? rho[r] / sg[r] : 0.0f;
+        float rp[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int s = 0; s < S; ++s)
+#pragma unroll
+          for (int r = 0; r < 4; ++r) {
+            dv[s][r] = fmaf(al[r], pv[s][r], dv[s][r]);
+            rv[s][r] = fmaf(-al[r], qv[s][r], rv[s][r]);
+            rp[r] = fmaf(rv[s][r], rv[s][r], rp[r]);
+          }
+        block_sum4(rp);
+        float be[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          be[r] = 0.0f;
+          if (iact[r]) {
+            total_iters[r] += 1;
+            if (!(rp[r] <= itol2 * rho0[r]) && isfinite(rp[r])) {
+              be[r] = rp[r] / rho[r];
+              rho[r] = rp[r];
+            } else {
+              iact[r] = false;
+            }
+          }
+        }
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+#pragma unroll
+          for (int r = 0; r < 4; ++r) pv[s][r] = fmaf(be[r], pv[s][r], rv[s][r]);
+          if (s < ns) st4(v32, g0 + s * P, pv[s]);
+        }
+        __syncthreads();
+      }
+      // ---- x~ += d (FP64), new FP64 residual r = -(A~ phi~)_I
+#pragma unroll
+      for (int s = 0; s < S; ++s)
+        if (s < ns) {
+          double xs[4];
+          ld4(v64, g0 + s * P, xs);
+#pragma unroll
+          for (int r = 0; r < 4; ++r) xs[r] += (double)dv[s][r];
+          st4(v64, g0 + s * P, xs);
+        }
+      __syncthreads();
+#pragma unroll
+      for (int s = 0; s < S; ++s)
+        if (s < ns) {
+          double y[4];
+          stencil9<double>(c64, v64, g0 + s * P, P, y);
+#pragma unroll
+          for (int r = 0; r < 4; ++r) r64[s][r] = -y[r];
+        }
     }
+    if (tid == 0) cs.refinements = ref;
+
+    // ---------------- epilogue ----------------------------------------
+    // interior: A~ phi~ = -r (the converged FP64 residual, in registers)
+    double acc[32];
+#pragma unroll
+    for (int i = 0; i < 32; ++i) acc[i] = 0.0;
+#pragma unroll
+    for (int s = 0; s < S; ++s)
+      if (s < ns) {
+        double ph[4], y[4];
+        ld4(v64, g0 + s * P, ph);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) y[r] = -r64[s][r];
+        epilogue_node(p, cs, d64, N, P, ix, s0 + s, ph, y, acc);
+      }
+    // boundary rows: stencil of the unconstrained matrix
+    for (int k = tid; k < 4 * N; k += NT) {
+      int bx, by;
+      boundary_node(k, N, bx, by);
+      const int g = (by + 1) * P + bx + 1;
+      double y[4], ph[4];
+      stencil9<double>(c64, v64, g, P, y);
+      ld4(v64, g, ph);
+      epilogue_node(p, cs, d64, N, P, bx, by, ph, y, acc);
+    }
+    write_basis<NT>(p, cell, N, v64, d64, tid);
+    __syncthreads();  // v32 is reused for the 32-value partials below
+    epilogue_finish<NT, true>(p, cs, cell, acc, reinterpret_cast<double *>(v32), true, total_iters, tid);
   }
 }
 

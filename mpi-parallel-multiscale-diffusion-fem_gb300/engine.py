@@ -137,6 +137,25 @@ class Engine:
             raise _abi.MsfemError(rc, _abi.last_error(self.lib))
         return rc, (st.as_dict() if st is not None else None)
 
+    def autotune(self, problem, precision="fp64", tol=1e-10, maxit=1000, sample_cells=1024):
+        """Pick the fastest compiled launch shape / parameters for this
+        problem's (dim, N class, precision); kept in the handle."""
+        keep = []
+        d = self.make_desc(problem, precision, tol, maxit, keep=keep)
+        t = _abi.Tuning()
+        rc = self.lib.msfem_autotune(self.handle, ctypes.byref(d), sample_cells, ctypes.byref(t))
+        if rc != _abi.OK:
+            raise _abi.MsfemError(rc, _abi.last_error(self.lib))
+        return t.as_dict()
+
+    def set_tuning(self, tuning):
+        t = _abi.Tuning()
+        for k, v in tuning.items():
+            setattr(t, k, v)
+        rc = self.lib.msfem_set_tuning(self.handle, ctypes.byref(t))
+        if rc != _abi.OK:
+            raise _abi.MsfemError(rc, _abi.last_error(self.lib))
+
     def tabulate(self, problem, ncomp):
         keep = []
         d = self.make_desc(problem, keep=keep)
