@@ -79,6 +79,7 @@ struct msfem_handle {
   DevBuf corners, nfine, order, queue, qp, qpoff, warm, boff, modes, spheres, sgrid_start, sgrid_ids;
   // outputs staged to the host / internal
   DevBuf M, F, basis, status, iters, relres, refine;
+  DevBuf work;  // per-CTA workspace slots of the 3D kernels
   // autotuned launch choices, keyed by (dim, N class, precision)
   std::map<int, Tune> tuning;
 };
@@ -280,19 +281,20 @@ struct Launch {
   const void *fn;
   int nt;
   size_t smem;
-  int rows;  // nodes per thread strip (mixed kernels), 0 otherwise
-  int minb;  // CTAs per SM the kernel was compiled for
+  int rows;          // nodes per thread strip (mixed kernels), 0 otherwise
+  int minb;          // CTAs per SM the kernel was compiled for
+  size_t slot_bytes; // per-CTA global workspace (3D kernels), 0 = none
 };
 
 template <int NMAX, int NT>
 Launch make2d() {
   return Launch{(const void *)msfem::msfem2d_kernel<NMAX, NT>, NT, msfem::Smem2D<NMAX>::bytes(false),
-                0, 2};
+                0, 2, 0};
 }
 template <int NMAX, int NT, int S, int MINB>
 Launch make2d_mixed() {
   return Launch{(const void *)msfem::msfem2d_mixed_kernel<NMAX, NT, S, MINB>, NT,
-                msfem::Smem2D<NMAX>::bytes(true), S, MINB};
+                msfem::Smem2D<NMAX>::bytes(true), S, MINB, 0};
 }
 
 // Compiled launch shapes per (dim, N class, precision); index 0 is the default.
@@ -312,9 +314,14 @@ std::vector<Launch> candidates(int dim, int nmax, bool mixed) {
     }
     return {};
   }
-  Launch l{};
-  if (msfem::pick3d_kernel(nmax, mixed, &l.fn, &l.nt, &l.smem) != 0) return {};
-  return {l};
+  if (nmax > MSFEM_MAX_N_3D) return {};
+  const size_t slot = msfem::Work3D::bytes(mixed);
+  if (mixed)
+    return {Launch{(const void *)msfem::msfem3d_kernel<256, true>, 256, 0, 0, 2, slot},
+            Launch{(const void *)msfem::msfem3d_kernel<512, true>, 512, 0, 0, 1, slot},
+            Launch{(const void *)msfem::msfem3d_kernel<256, true>, 256, 0, 0, 4, slot}};
+  return {Launch{(const void *)msfem::msfem3d_kernel<256, false>, 256, 0, 0, 2, slot},
+          Launch{(const void *)msfem::msfem3d_kernel<512, false>, 512, 0, 0, 1, slot}};
 }
 
 int size_class(int dim, int nmax) {
@@ -639,7 +646,8 @@ int msfem_destroy(msfem_handle *h) {
   cudaStreamSynchronize(h->stream);
   DevBuf *bufs[] = {&h->corners, &h->nfine, &h->order, &h->queue, &h->qp, &h->qpoff, &h->warm,
                     &h->boff, &h->modes, &h->spheres, &h->sgrid_start, &h->sgrid_ids,
-                    &h->M, &h->F, &h->basis, &h->status, &h->iters, &h->relres, &h->refine};
+                    &h->M, &h->F, &h->basis, &h->status, &h->iters, &h->relres, &h->refine,
+                    &h->work};
   for (DevBuf *b : bufs) b->release();
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
@@ -881,16 +889,25 @@ int run_batch_impl(msfem_handle *h, const msfem_batch_desc *d, double *M, double
   p.queue = h->queue.as<unsigned int>();
 
   // ---- launch: persistent CTAs, size-sorted work queue
-  MSFEM_CUDA(cudaFuncSetAttribute(L.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem));
+  if (L.smem > 0)
+    MSFEM_CUDA(cudaFuncSetAttribute(L.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem));
   int per_sm = 0;
   MSFEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, L.fn, L.nt, L.smem));
   if (per_sm < 1) return fail(MSFEM_ERR_UNSUPPORTED, "kernel does not fit on an SM");
+  if (L.slot_bytes) per_sm = std::min(per_sm, L.minb);  // workspace slots per SM
   const int grid = std::max(1, std::min(nc, per_sm * h->sm_count));
+  unsigned char *work = nullptr;
+  size_t slot_bytes = L.slot_bytes;
+  if (slot_bytes) {
+    MSFEM_CUDA(h->work.ensure(slot_bytes * grid));
+    work = h->work.as<unsigned char>();
+  }
   MSFEM_CUDA(cudaMemsetAsync(p.queue, 0, sizeof(unsigned int), h->stream));
   MSFEM_CUDA(cudaEventRecord(h->ev0, h->stream));
   if (nc > 0) {
-    void *args[] = {&p};
-    MSFEM_CUDA(cudaLaunchKernel(L.fn, dim3(grid), dim3(L.nt), args, L.smem, h->stream));
+    void *args2[] = {&p};
+    void *args3[] = {&p, &work, &slot_bytes};
+    MSFEM_CUDA(cudaLaunchKernel(L.fn, dim3(grid), dim3(L.nt), slot_bytes ? args3 : args2, L.smem, h->stream));
     launches++;
   }
   MSFEM_CUDA(cudaEventRecord(h->ev1, h->stream));

@@ -1,13 +1,948 @@
-// msfem_kernel3d.cuh -- 3D multiscale-basis kernels (not yet built).
+// msfem_kernel3d.cuh -- 3D multiscale-basis kernels for sm_103a.
+//
+// Same algorithm as the 2D kernels (diffusion_problem_basis.tpp:159-285):
+// QGauss(2) trilinear Q1 assembly into a 27-point node stencil (8-colour
+// scatter, no atomics), symmetric D^-1/2 scaling, all 8 Dirichlet problems
+// (coarse trilinear nodal functions, basis_q1.tpp:50-75) advanced together by
+// CG with per-RHS relative stopping, and the M = phi^T A phi / F = phi^T b
+// epilogue.  FP64 form and mixed form (FP32 inner CG, FP64 residual
+// refinement) as in 2D.
+//
+// A 3D local problem with 8 right-hand sides does not fit one SM's shared
+// memory (N = 24: 15625 nodes x 176 B in FP64), so each persistent CTA owns
+// a slot of a global-memory workspace with structure-of-arrays vectors
+// ([component][node], coalesced along x).  The working set of one sweep
+// (three node planes) stays in L1; the couplings stream from L2.  Bound: the
+// FP64 pipe in the FP64 form (26 FMA x 8 RHS per node per iteration against
+// ~100 B of couplings), L1/L2 bandwidth in the FP32 inner loop.
+//
+// Node (ix,iy,iz) of the (N+1)^3 grid sits at g = ((iz+1) P + iy + 1) P + ix + 1,
+// P = N + 3 (a zero ring around the grid).  Each node stores its 13 "forward"
+// couplings (offsets lexicographically after it); the 13 backward ones are
+// the forward couplings of the neighbours.
 #pragma once
 
 #include "msfem_common.cuh"
 
 namespace msfem {
 
-inline int pick3d_kernel(int nmax, bool mixed, const void **fn, int *nt, size_t *smem) {
-  (void)nmax; (void)mixed; (void)fn; (void)nt; (void)smem;
-  return -1;
+constexpr int kNMax3D = MSFEM_MAX_N_3D;
+
+// Per-slot workspace layout (in units of G = P^3 values, P = NMAX + 3).
+struct Work3D {
+  static constexpr int P = kNMax3D + 3;
+  static constexpr long G = (long)P * P * P;
+  // FP64 arrays
+  static constexpr long kC64 = 0;              // [13][G] scaled couplings
+  static constexpr long kD64 = kC64 + 13 * G;  // [G] diagonal
+  static constexpr long kX64 = kD64 + G;       // [8][G] phi~ (boundary g~, interior x~)
+  static constexpr long kR64 = kX64 + 8 * G;   // [8][G] residual (FP64 CG) / scratch
+  static constexpr long kP64 = kR64 + 8 * G;   // [8][G] search direction (FP64 CG)
+  static constexpr long kQ64 = kP64 + 8 * G;   // [8][G] A p
+  static constexpr long kEnd64 = kQ64 + 8 * G;
+  // FP32 arrays (mixed form)
+  static constexpr long kC32 = 0;              // [13][G]
+  static constexpr long kD32 = kC32 + 13 * G;  // [8][G] correction d
+  static constexpr long kR32 = kD32 + 8 * G;   // [8][G]
+  static constexpr long kP32 = kR32 + 8 * G;   // [8][G]
+  static constexpr long kQ32 = kP32 + 8 * G;   // [8][G]
+  static constexpr long kEnd32 = kQ32 + 8 * G;
+  // every slot starts on a 256-byte boundary (slot k at k * bytes())
+  static constexpr size_t bytes(bool mixed) {
+    return (sizeof(double) * kEnd64 + (mixed ? sizeof(float) * kEnd32 : 0) + 511) & ~size_t(255);
+  }
+  static_assert((sizeof(double) * kEnd64) % 16 == 0, "FP32 arrays start aligned");
+};
+
+// Forward offsets: (1,0,0), (-1..1,1,0), (-1..1,-1..1,1).
+__device__ __forceinline__ void fwd_offset(int o, int &dx, int &dy, int &dz) {
+  if (o == 0) { dx = 1; dy = 0; dz = 0; }
+  else if (o < 4) { dx = o - 2; dy = 1; dz = 0; }
+  else { const int m = o - 4; dx = m % 3 - 1; dy = m / 3 - 1; dz = 1; }
+}
+__device__ __forceinline__ int fwd_index(int dx, int dy, int dz) {
+  if (dz == 1) return 4 + (dy + 1) * 3 + (dx + 1);
+  if (dy == 1) return 1 + (dx + 1);
+  return 0;  // (1,0,0)
+}
+__device__ __forceinline__ bool is_forward(int dx, int dy, int dz) {
+  return dz > 0 || (dz == 0 && (dy > 0 || (dy == 0 && dx > 0)));
+}
+
+struct CellShared3D {
+  double corners[24];
+  double q1coef[64];
+  double q1shift[3];
+  double q1iscale;
+  double jinv[9];      // affine: inverse fine Jacobian (row-major)
+  double jfine[9];     // affine: fine Jacobian, column a = dx/dxi_a
+  double absdet;
+  double tmpl[8][36];  // affine scalar coefficient: K = sum_q a_q tmpl[q] (upper triangle)
+  double bb[8];
+  double nu[8];
+  double rho[8];
+  double alpha[8];
+  double beta[8];
+  double dmin;
+  int active[8];
+  int iters[8];
+  int offs[13];        // grid offsets of the forward couplings
+  int status;
+  int affine;
+  int need_nu;
+  int done;
+  int cell;
+  int refinements;
+};
+
+__device__ __forceinline__ void trilinear_map(const double *cr, const double *t, double *x) {
+  x[0] = x[1] = x[2] = 0.0;
+#pragma unroll
+  for (int v = 0; v < 8; ++v) {
+    const double w = ((v & 1) ? t[0] : 1.0 - t[0]) * ((v & 2) ? t[1] : 1.0 - t[1]) *
+                     ((v & 4) ? t[2] : 1.0 - t[2]);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) x[a] = fma(w, cr[3 * v + a], x[a]);
+  }
+}
+
+__device__ __forceinline__ double gp3(int i) {
+  return i ? 0.78867513459481288225457439025098 : 0.21132486540518711774542560974902;
+}
+__device__ __forceinline__ double lv3(int b, int q) { return b ? gp3(q) : gp3(1 - q); }
+
+// reference gradient of vertex k at Gauss point q (component a)
+__device__ __forceinline__ double rgrad(int k, int q, int a) {
+  double g = ((k >> a) & 1) ? 1.0 : -1.0;
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    if (c != a) g *= lv3((k >> c) & 1, (q >> c) & 1);
+  return g;
+}
+
+__device__ __forceinline__ int tri_index(int i, int j) {  // i <= j < 8
+  return i * 8 - i * (i - 1) / 2 + (j - i);
+}
+
+// Element matrix (upper triangle, 36 entries) of fine cell (cx,cy,cz).
+__device__ bool element3d(const KernelParams &p, const CellShared3D &cs, const double *__restrict__ tab,
+                          int N, int cx, int cy, int cz, bool scalar, bool need_x, double (&K)[36]) {
+  const int nfc = N * N * N, fc = cx + N * (cy + N * cz);
+#pragma unroll
+  for (int e = 0; e < 36; ++e) K[e] = 0.0;
+  if (cs.affine && scalar) {
+#pragma unroll 1
+    for (int q = 0; q < 8; ++q) {
+      double xq[3] = {0.0, 0.0, 0.0}, A[6];
+      if (need_x) {
+        const double u[3] = {cx + gp3(q & 1), cy + gp3((q >> 1) & 1), cz + gp3(q >> 2)};
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+          xq[a] = cs.corners[a] + cs.jfine[3 * a] * u[0] + cs.jfine[3 * a + 1] * u[1] + cs.jfine[3 * a + 2] * u[2];
+      }
+      coef_at<3>(p, xq, tab, q, nfc, fc, A);
+      const double a = A[0];
+#pragma unroll
+      for (int e = 0; e < 36; ++e) K[e] = fma(a, cs.tmpl[q][e], K[e]);
+    }
+    return true;
+  }
+  // general path: per-Gauss-point Jacobian and tensor coefficient
+  const double invN = 1.0 / (double)N;
+  double V[24];
+#pragma unroll 1
+  for (int k = 0; k < 8; ++k) {
+    const double t[3] = {(cx + (k & 1)) * invN, (cy + ((k >> 1) & 1)) * invN, (cz + (k >> 2)) * invN};
+    trilinear_map(cs.corners, t, V + 3 * k);
+  }
+  bool ok = true;
+#pragma unroll 1
+  for (int q = 0; q < 8; ++q) {
+    double J[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, xq[3] = {0.0, 0.0, 0.0};
+    for (int k = 0; k < 8; ++k) {
+      const double psi = lv3(k & 1, q & 1) * lv3((k >> 1) & 1, (q >> 1) & 1) * lv3(k >> 2, q >> 2);
+      for (int a = 0; a < 3; ++a) {
+        xq[a] += psi * V[3 * k + a];
+        for (int c = 0; c < 3; ++c) J[3 * a + c] += V[3 * k + a] * rgrad(k, q, c);
+      }
+    }
+    const double c00 = J[4] * J[8] - J[5] * J[7], c01 = J[5] * J[6] - J[3] * J[8],
+                 c02 = J[3] * J[7] - J[4] * J[6];
+    const double det = J[0] * c00 + J[1] * c01 + J[2] * c02;
+    if (!(det > 0.0)) ok = false;
+    const double id = 1.0 / det;
+    double Ji[9];
+    Ji[0] = c00 * id; Ji[1] = (J[2] * J[7] - J[1] * J[8]) * id; Ji[2] = (J[1] * J[5] - J[2] * J[4]) * id;
+    Ji[3] = c01 * id; Ji[4] = (J[0] * J[8] - J[2] * J[6]) * id; Ji[5] = (J[2] * J[3] - J[0] * J[5]) * id;
+    Ji[6] = c02 * id; Ji[7] = (J[1] * J[6] - J[0] * J[7]) * id; Ji[8] = (J[0] * J[4] - J[1] * J[3]) * id;
+    double A6[6];
+    coef_at<3>(p, xq, tab, q, nfc, fc, A6);
+    const double A[9] = {A6[0], A6[1], A6[2], A6[1], A6[3], A6[4], A6[2], A6[4], A6[5]};
+    const double w = 0.125 * fabs(det);
+    double G[8][3];  // physical gradients
+    for (int k = 0; k < 8; ++k)
+      for (int a = 0; a < 3; ++a) {
+        double s = 0.0;
+        for (int c = 0; c < 3; ++c) s += Ji[3 * c + a] * rgrad(k, q, c);
+        G[k][a] = s;
+      }
+    for (int j = 0; j < 8; ++j) {
+      double AG[3];
+      for (int a = 0; a < 3; ++a) AG[a] = A[3 * a] * G[j][0] + A[3 * a + 1] * G[j][1] + A[3 * a + 2] * G[j][2];
+      for (int i = 0; i <= j; ++i)
+        K[tri_index(i, j)] += w * (G[i][0] * AG[0] + G[i][1] * AG[1] + G[i][2] * AG[2]);
+    }
+  }
+  return ok;
+}
+
+// y = A~ v at node g for 8 RHS (SoA vectors with stride G).
+template <typename T>
+__device__ __forceinline__ void stencil27(const T *__restrict__ c, const T *__restrict__ v, long G,
+                                          const int *offs, int g, T (&y)[8]) {
+#pragma unroll
+  for (int r = 0; r < 8; ++r) y[r] = v[r * G + g];
+#pragma unroll 1
+  for (int o = 0; o < 13; ++o) {
+    const int d = offs[o];
+    const T cf = c[o * G + g];
+    const T cb = c[o * G + g - d];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      y[r] = fma(cf, v[r * G + g + d], y[r]);
+      y[r] = fma(cb, v[r * G + g - d], y[r]);
+    }
+  }
+}
+
+__device__ __forceinline__ int grid3(int P, int ix, int iy, int iz) { return ((iz + 1) * P + iy + 1) * P + ix + 1; }
+
+template <int NT, bool MIXED>
+__global__ void __launch_bounds__(NT)
+msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t slot_bytes) {
+  constexpr int NW = NT / 32;
+  __shared__ CellShared3D cs;
+  __shared__ double red[2][NW * 16];
+  __shared__ double redE[NW * 32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  unsigned char *slot = work + (size_t)blockIdx.x * slot_bytes;
+  double *W64 = reinterpret_cast<double *>(slot);
+  float *W32 = reinterpret_cast<float *>(slot + sizeof(double) * Work3D::kEnd64);
+
+  for (;;) {
+    if (tid == 0) {
+      const unsigned wi = atomicAdd(p.queue, 1u);
+      cs.cell = wi < (unsigned)p.n_cells ? (p.order ? p.order[wi] : (int)wi) : -1;
+    }
+    __syncthreads();
+    const int cell = cs.cell;
+    if (cell < 0) break;
+    const int N = p.n_fine ? p.n_fine[cell] : p.n_fine_uniform;
+    const int P = N + 3, n = N + 1, m = N - 1;
+    const long G = (long)P * P * P;
+    const int nI = m * m * m, nn = n * n * n;
+    double *c64 = W64 + Work3D::kC64 * 0 + 0;  // strides use this cell's G
+    double *d64 = c64 + 13 * G;
+    double *x64 = d64 + G;
+    double *r64 = x64 + 8 * G;
+    double *p64 = r64 + 8 * G;
+    double *q64 = p64 + 8 * G;
+    float *c32 = W32;
+    float *dd32 = c32 + 13 * G;
+    float *rr32 = dd32 + 8 * G;
+    float *pp32 = rr32 + 8 * G;
+    float *qq32 = pp32 + 8 * G;
+
+    // ---------------- set-up ------------------------------------------
+    if (tid < 24) cs.corners[tid] = p.corners[(int64_t)cell * 24 + tid];
+    if (tid < 13) {
+      int dx, dy, dz;
+      fwd_offset(tid, dx, dy, dz);
+      cs.offs[tid] = (dz * P + dy) * P + dx;
+    }
+    if (tid < 8) { cs.iters[tid] = 0; cs.active[tid] = 1; cs.nu[tid] = 0.0; }
+    for (long i = tid; i < 22 * G; i += NT) c64[i] = 0.0;  // couplings, diagonal, phi~
+    __syncthreads();
+    if (tid == 0) {
+      const double *cr = cs.corners;
+      int st = MSFEM_CELL_CONVERGED;
+      if (N < 1 || N > kNMax3D) st = MSFEM_CELL_BAD_INPUT;
+      if (st == MSFEM_CELL_CONVERGED && !q1_setup<3>(cr, cs.q1coef, cs.q1shift, &cs.q1iscale))
+        st = MSFEM_CELL_BAD_INPUT;
+      // parallelepiped: v_k = v0 + kx e1 + ky e2 + kz e3 exactly
+      int aff = 1;
+      for (int k = 0; k < 8 && aff; ++k)
+        for (int a = 0; a < 3; ++a) {
+          const double pred = cr[a] + ((k & 1) ? cr[3 + a] - cr[a] : 0.0) + ((k & 2) ? cr[6 + a] - cr[a] : 0.0) +
+                              ((k & 4) ? cr[12 + a] - cr[a] : 0.0);
+          if (pred != cr[3 * k + a]) aff = 0;
+        }
+      cs.affine = aff;
+      cs.refinements = 0;
+      if (aff && st == MSFEM_CELL_CONVERGED) {
+        const double invN = 1.0 / (double)N;
+        double J[9];
+        for (int a = 0; a < 3; ++a) {
+          J[3 * a + 0] = (cr[3 + a] - cr[a]) * invN;
+          J[3 * a + 1] = (cr[6 + a] - cr[a]) * invN;
+          J[3 * a + 2] = (cr[12 + a] - cr[a]) * invN;
+        }
+        const double c00 = J[4] * J[8] - J[5] * J[7], c01 = J[5] * J[6] - J[3] * J[8],
+                     c02 = J[3] * J[7] - J[4] * J[6];
+        const double det = J[0] * c00 + J[1] * c01 + J[2] * c02;
+        if (!(det > 0.0)) st = MSFEM_CELL_BAD_INPUT;
+        const double id = 1.0 / det;
+        cs.jinv[0] = c00 * id; cs.jinv[1] = (J[2] * J[7] - J[1] * J[8]) * id; cs.jinv[2] = (J[1] * J[5] - J[2] * J[4]) * id;
+        cs.jinv[3] = c01 * id; cs.jinv[4] = (J[0] * J[8] - J[2] * J[6]) * id; cs.jinv[5] = (J[2] * J[3] - J[0] * J[5]) * id;
+        cs.jinv[6] = c02 * id; cs.jinv[7] = (J[1] * J[6] - J[0] * J[7]) * id; cs.jinv[8] = (J[0] * J[4] - J[1] * J[3]) * id;
+        for (int e = 0; e < 9; ++e) cs.jfine[e] = J[e];
+        cs.absdet = fabs(det);
+      }
+      cs.status = st;
+    }
+    __syncthreads();
+    // element templates for a scalar coefficient on an affine cell:
+    // tmpl[q](i,j) = w|det| (Ji^T grad_i) . (Ji^T grad_j) at Gauss point q
+    const bool scalar = (p.coef_kind == MSFEM_COEF_TABULATED && p.ncomp == 1) ||
+                        p.coef_kind == MSFEM_COEF_SINSIN;
+    if (cs.status == MSFEM_CELL_CONVERGED && cs.affine && scalar) {
+      for (int e = tid; e < 8 * 36; e += NT) {
+        const int q = e / 36, t = e % 36;
+        int i = 0, rem = t;
+        while (rem >= 8 - i) { rem -= 8 - i; ++i; }
+        const int j = i + rem;
+        double gi[3], gj[3];
+        for (int a = 0; a < 3; ++a) {
+          double si = 0.0, sj = 0.0;
+          for (int c = 0; c < 3; ++c) {
+            si += cs.jinv[3 * c + a] * rgrad(i, q, c);
+            sj += cs.jinv[3 * c + a] * rgrad(j, q, c);
+          }
+          gi[a] = si;
+          gj[a] = sj;
+        }
+        cs.tmpl[q][t] = 0.125 * cs.absdet * (gi[0] * gj[0] + gi[1] * gj[1] + gi[2] * gj[2]);
+      }
+    }
+    __syncthreads();
+    if (cs.status != MSFEM_CELL_CONVERGED) {
+      for (int i = tid; i < 64; i += NT) p.M[(int64_t)cell * 64 + i] = __longlong_as_double(0x7ff8000000000000ll);
+      if (tid < 8) {
+        p.F[(int64_t)cell * 8 + tid] = __longlong_as_double(0x7ff8000000000000ll);
+        if (p.iters) p.iters[(int64_t)cell * 8 + tid] = 0;
+      }
+      if (tid == 0) {
+        p.status[cell] = cs.status;
+        if (p.rel_res) p.rel_res[cell] = __longlong_as_double(0x7ff8000000000000ll);
+        if (p.refinements) p.refinements[cell] = 0;
+      }
+      __syncthreads();
+      continue;
+    }
+
+    // ---------------- assembly: 8-colour scatter -------------------------
+    {
+      const int nfc = N * N * N;
+      const double *tab = nullptr;
+      if (p.coef_kind == MSFEM_COEF_TABULATED)
+        tab = p.qp_values + (p.qp_offset ? p.qp_offset[cell] : (int64_t)cell * p.ncomp * 8 * nfc);
+      const bool need_x = p.coef_kind != MSFEM_COEF_TABULATED && p.coef_kind != MSFEM_COEF_CONSTANT;
+      for (int col = 0; col < 8; ++col) {
+        const int ox = col & 1, oy = (col >> 1) & 1, oz = col >> 2;
+        const int nx = (N - ox + 1) >> 1, ny = (N - oy + 1) >> 1, nz = (N - oz + 1) >> 1;
+        for (int idx = tid; idx < nx * ny * nz; idx += NT) {
+          const int cx = ox + 2 * (idx % nx), cy = oy + 2 * ((idx / nx) % ny), cz = oz + 2 * (idx / (nx * ny));
+          double K[36];
+          if (!element3d(p, cs, tab, N, cx, cy, cz, scalar, need_x, K)) cs.status = MSFEM_CELL_BAD_INPUT;
+          const int g0 = grid3(P, cx, cy, cz);
+#pragma unroll 1
+          for (int i = 0; i < 8; ++i) {
+            const int gi = g0 + ((i >> 2) * P + ((i >> 1) & 1)) * P + (i & 1);
+            d64[gi] += K[tri_index(i, i)];
+            for (int j = i + 1; j < 8; ++j) {
+              int dx = (j & 1) - (i & 1), dy = ((j >> 1) & 1) - ((i >> 1) & 1), dz = (j >> 2) - (i >> 2);
+              int base = gi;
+              if (!is_forward(dx, dy, dz)) {
+                base = gi + (dz * P + dy) * P + dx;
+                dx = -dx; dy = -dy; dz = -dz;
+              }
+              c64[(long)fwd_index(dx, dy, dz) * G + base] += K[tri_index(i, j)];
+            }
+          }
+        }
+        __syncthreads();
+      }
+    }
+    if (cs.status != MSFEM_CELL_CONVERGED) {
+      for (int i = tid; i < 64; i += NT) p.M[(int64_t)cell * 64 + i] = __longlong_as_double(0x7ff8000000000000ll);
+      if (tid < 8) {
+        p.F[(int64_t)cell * 8 + tid] = __longlong_as_double(0x7ff8000000000000ll);
+        if (p.iters) p.iters[(int64_t)cell * 8 + tid] = 0;
+      }
+      if (tid == 0) {
+        p.status[cell] = cs.status;
+        if (p.rel_res) p.rel_res[cell] = __longlong_as_double(0x7ff8000000000000ll);
+        if (p.refinements) p.refinements[cell] = 0;
+      }
+      __syncthreads();
+      continue;
+    }
+
+    // ---------------- symmetric scaling, Dirichlet data --------------------
+    // D^-1/2 temporarily in r64[0]
+    double dmin_part = 1e300;
+    for (int k = tid; k < nn; k += NT) {
+      const int ix = k % n, iy = (k / n) % n, iz = k / (n * n);
+      const int g = grid3(P, ix, iy, iz);
+      const double d = d64[g];
+      r64[g] = rsqrt(d);
+      if (ix > 0 && iy > 0 && iz > 0 && ix < N && iy < N && iz < N) {
+        dmin_part = fmin(dmin_part, d);
+        if (!(d > 0.0) || !isfinite(d)) cs.status = MSFEM_CELL_NAN;
+      }
+    }
+    // zero the ring entries of the temporary (read by the scaling below)
+    for (long i = tid; i < G; i += NT) {
+      const int ix = (int)(i % P) - 1, iy = (int)((i / P) % P) - 1, iz = (int)(i / ((long)P * P)) - 1;
+      if (ix < 0 || iy < 0 || iz < 0 || ix > N || iy > N || iz > N) r64[i] = 0.0;
+    }
+    __syncthreads();
+    for (int k = tid; k < nn; k += NT) {
+      const int ix = k % n, iy = (k / n) % n, iz = k / (n * n);
+      const int g = grid3(P, ix, iy, iz);
+      const double s = r64[g];
+#pragma unroll 1
+      for (int o = 0; o < 13; ++o) c64[o * G + g] *= s * r64[g + cs.offs[o]];
+    }
+#pragma unroll
+    for (int mm = 16; mm >= 1; mm >>= 1) dmin_part = fmin(dmin_part, shfl_xor_d(dmin_part, mm));
+    if (lane == 0) red[0][warp] = dmin_part;
+    __syncthreads();
+    for (int k = tid; k < nn; k += NT) {
+      const int ix = k % n, iy = (k / n) % n, iz = k / (n * n);
+      const int g = grid3(P, ix, iy, iz);
+      if (ix == 0 || iy == 0 || iz == 0 || ix == N || iy == N || iz == N) {
+        const double t[3] = {ix / (double)N, iy / (double)N, iz / (double)N};
+        double x[3], gv[8];
+        trilinear_map(cs.corners, t, x);
+        q1_eval<3>(cs.q1coef, cs.q1shift, cs.q1iscale, x, gv);
+        const double sq = d64[g] * r64[g];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) x64[r * G + g] = gv[r] * sq;
+      }
+    }
+    if (tid == 0) {
+      double mn = 1e300;
+      for (int w = 0; w < NW; ++w) mn = fmin(mn, red[0][w]);
+      cs.dmin = mn;
+    }
+    __syncthreads();
+
+    // interior node k -> grid index
+    auto interior = [&](int k) {
+      const int ix = 1 + k % m, iy = 1 + (k / m) % m, iz = 1 + k / (m * m);
+      return grid3(P, ix, iy, iz);
+    };
+
+    // ---------------- right-hand sides b~ = -(A~ phi~)_I ---------------------
+    {
+      double bbp[8];
+#pragma unroll
+      for (int r = 0; r < 8; ++r) bbp[r] = 0.0;
+      for (int k = tid; k < nI; k += NT) {
+        const int g = interior(k);
+        double y[8];
+        stencil27<double>(c64, x64, G, cs.offs, g, y);
+        const double d = d64[g];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+          r64[r * G + g] = -y[r];
+          bbp[r] = fma(y[r] * d, y[r], bbp[r]);
+        }
+      }
+      const double t = warp_transpose_reduce<8>(bbp, lane);
+      if ((lane & 3) == 0) red[1][warp * 8 + (lane >> 2)] = t;
+      __syncthreads();
+      if (warp == 0) {
+        double s = 0.0;
+        for (int i = lane; i < NW * 8; i += 32) s += red[1][i];
+#pragma unroll
+        for (int mm = 8; mm < 32; mm <<= 1) s += shfl_xor_d(s, mm);
+        if (lane < 8) cs.bb[lane] = s;
+      }
+    }
+    // warm start: x~0 = D^1/2 phi_warm, r = -(A~ phi~0)_I
+    if (p.warm_basis != nullptr) {
+      const double *wb = p.warm_basis + (p.basis_offset ? p.basis_offset[cell] : (int64_t)cell * 8 * nn);
+      __syncthreads();
+      for (int k = tid; k < nI; k += NT) {
+        const int g = interior(k);
+        const int ix = 1 + k % m, iy = 1 + (k / m) % m, iz = 1 + k / (m * m);
+        const int node = (iz * n + iy) * n + ix;
+        const double sq = sqrt(d64[g]);
+#pragma unroll
+        for (int r = 0; r < 8; ++r) x64[r * G + g] = __ldg(wb + (int64_t)r * nn + node) * sq;
+      }
+      __syncthreads();
+      for (int k = tid; k < nI; k += NT) {
+        const int g = interior(k);
+        double y[8];
+        stencil27<double>(c64, x64, G, cs.offs, g, y);
+#pragma unroll
+        for (int r = 0; r < 8; ++r) r64[r * G + g] = -y[r];
+      }
+    }
+    __syncthreads();
+    const double tol2 = p.tol * p.tol;
+    int total_iters[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+
+    // 8-value block reduction finished by warp 0; returns after the barrier
+    // with the totals in red[buf] lanes 0..7 read by every thread through cs
+    if (!MIXED) {
+      // ================= plain FP64 CG (vectors in the workspace) ==========
+      // p = r on the interior, 0 on boundary and ring
+      for (long i = tid; i < 8 * G; i += NT) p64[i] = 0.0;
+      __syncthreads();
+      double rp[16];
+#pragma unroll
+      for (int r = 0; r < 16; ++r) rp[r] = 0.0;
+      for (int k = tid; k < nI; k += NT) {
+        const int g = interior(k);
+        const double d = d64[g];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+          const double rv = r64[r * G + g];
+          p64[r * G + g] = rv;
+          rp[r] = fma(rv, rv, rp[r]);
+          rp[8 + r] = fma(rv * d, rv, rp[8 + r]);
+        }
+      }
+      {
+        const double t = warp_transpose_reduce<16>(rp, lane);
+        if ((lane & 1) == 0) red[0][warp * 16 + (lane >> 1)] = t;
+      }
+      __syncthreads();
+      if (warp == 0) {
+        double s = 0.0;
+        for (int i = lane; i < NW * 16; i += 32) s += red[0][i];
+        s += shfl_xor_d(s, 16);
+        const double nu = shfl_xor_d(s, 8);
+        if (lane < 8) {
+          cs.rho[lane] = s;
+          cs.active[lane] = !(nu <= tol2 * cs.bb[lane]);
+          cs.iters[lane] = 0;
+        }
+        __syncwarp();
+        if (lane == 0) {
+          int any = 0, nn2 = 0;
+          for (int r = 0; r < 8; ++r) {
+            any |= cs.active[r];
+            if (cs.active[r] && cs.dmin * cs.rho[r] <= 100.0 * tol2 * cs.bb[r]) nn2 = 1;
+          }
+          cs.done = !any;
+          cs.need_nu = nn2 || p.check_interval == 1;
+        }
+      }
+      __syncthreads();
+      int it = 0;
+      while (!cs.done) {
+        ++it;
+        double sg[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) sg[r] = 0.0;
+        for (int k = tid; k < nI; k += NT) {
+          const int g = interior(k);
+          double y[8];
+          stencil27<double>(c64, p64, G, cs.offs, g, y);
+#pragma unroll
+          for (int r = 0; r < 8; ++r) {
+            q64[r * G + g] = y[r];
+            sg[r] = fma(p64[r * G + g], y[r], sg[r]);
+          }
+        }
+        {
+          const double t = warp_transpose_reduce<8>(sg, lane);
+          if ((lane & 3) == 0) red[1][warp * 8 + (lane >> 2)] = t;
+        }
+        __syncthreads();
+        if (warp == 0) {
+          double s = 0.0;
+          for (int i = lane; i < NW * 8; i += 32) s += red[1][i];
+#pragma unroll
+          for (int mm = 8; mm < 32; mm <<= 1) s += shfl_xor_d(s, mm);
+          if (lane < 8) {
+            double a = 0.0;
+            if (cs.active[lane]) {
+              if (cs.rho[lane] == 0.0) {
+                cs.active[lane] = 0;
+                cs.iters[lane] = it - 1;
+              } else {
+                a = cs.rho[lane] / s;
+                if (!isfinite(a) || !(s > 0.0)) {
+                  a = 0.0;
+                  cs.active[lane] = 0;
+                  cs.iters[lane] = -it;
+                }
+              }
+            }
+            cs.alpha[lane] = a;
+          }
+        }
+        __syncthreads();
+        const bool need_nu = cs.need_nu;
+        double al[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) al[r] = cs.alpha[r];
+#pragma unroll
+        for (int r = 0; r < 16; ++r) rp[r] = 0.0;
+        for (int k = tid; k < nI; k += NT) {
+          const int g = interior(k);
+          const double d = d64[g];
+#pragma unroll
+          for (int r = 0; r < 8; ++r) {
+            const double pv = p64[r * G + g];
+            x64[r * G + g] = fma(al[r], pv, x64[r * G + g]);
+            const double rv = fma(-al[r], q64[r * G + g], r64[r * G + g]);
+            r64[r * G + g] = rv;
+            rp[r] = fma(rv, rv, rp[r]);
+            if (need_nu) rp[8 + r] = fma(rv * d, rv, rp[8 + r]);
+          }
+        }
+        {
+          const double t = warp_transpose_reduce<16>(rp, lane);
+          if ((lane & 1) == 0) red[0][warp * 16 + (lane >> 1)] = t;
+        }
+        __syncthreads();
+        if (warp == 0) {
+          double s = 0.0;
+          for (int i = lane; i < NW * 16; i += 32) s += red[0][i];
+          s += shfl_xor_d(s, 16);
+          const double nu = shfl_xor_d(s, 8);
+          if (lane < 8) {
+            double b = 0.0;
+            if (cs.active[lane]) {
+              if (!isfinite(s)) {
+                cs.active[lane] = 0;
+                cs.iters[lane] = -it;
+              } else if (s == 0.0 || (need_nu && nu <= tol2 * cs.bb[lane])) {
+                cs.active[lane] = 0;
+                cs.iters[lane] = it;
+              } else if (it >= p.maxit) {
+                cs.active[lane] = 0;
+                cs.iters[lane] = -1000000 - it;
+              } else {
+                b = s / cs.rho[lane];
+                cs.rho[lane] = s;
+              }
+            }
+            cs.beta[lane] = b;
+          }
+          __syncwarp();
+          if (lane == 0) {
+            int any = 0, nn2 = 0;
+            for (int r = 0; r < 8; ++r) {
+              any |= cs.active[r];
+              if (cs.active[r] && cs.dmin * cs.rho[r] <= 100.0 * tol2 * cs.bb[r]) nn2 = 1;
+            }
+            cs.done = !any;
+            cs.need_nu = nn2 || (p.check_interval > 0 && ((it + 1) % p.check_interval) == 0);
+          }
+        }
+        __syncthreads();
+        if (cs.done) break;
+        double be[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) be[r] = cs.beta[r];
+        for (int k = tid; k < nI; k += NT) {
+          const int g = interior(k);
+#pragma unroll
+          for (int r = 0; r < 8; ++r) p64[r * G + g] = fma(be[r], p64[r * G + g], r64[r * G + g]);
+        }
+        __syncthreads();
+      }
+    } else {
+      // ================= MIXED: FP32 inner CG + FP64 refinement ===========
+      for (long i = tid; i < 13 * G; i += NT) c32[i] = (float)c64[i];
+      for (long i = tid; i < 8 * G; i += NT) pp32[i] = 0.0f;
+      __syncthreads();
+      const float itol2 = p.inner_tol * p.inner_tol;
+      int ref = 0;
+      for (;;) {
+        double nup[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) nup[r] = 0.0;
+        for (int k = tid; k < nI; k += NT) {
+          const int g = interior(k);
+          const double d = d64[g];
+#pragma unroll
+          for (int r = 0; r < 8; ++r) {
+            const double rv = r64[r * G + g];
+            nup[r] = fma(rv * d, rv, nup[r]);
+          }
+        }
+        {
+          const double t = warp_transpose_reduce<8>(nup, lane);
+          if ((lane & 3) == 0) red[0][warp * 8 + (lane >> 2)] = t;
+        }
+        __syncthreads();
+        if (warp == 0) {
+          double s = 0.0;
+          for (int i = lane; i < NW * 8; i += 32) s += red[0][i];
+#pragma unroll
+          for (int mm = 8; mm < 32; mm <<= 1) s += shfl_xor_d(s, mm);
+          if (lane < 8) {
+            cs.nu[lane] = s;
+            if (!isfinite(s)) {
+              cs.active[lane] = 0;
+              cs.iters[lane] = -1;
+            } else {
+              cs.active[lane] = !(s <= tol2 * cs.bb[lane]);
+            }
+          }
+          __syncwarp();
+          if (lane == 0) {
+            int any = 0;
+            for (int r = 0; r < 8; ++r) any |= cs.active[r];
+            if (any && ref >= p.max_refine) {
+              for (int r = 0; r < 8; ++r)
+                if (cs.active[r]) { cs.active[r] = 0; cs.iters[r] = -1000000; }
+              any = 0;
+            }
+            cs.done = !any;
+          }
+        }
+        __syncthreads();
+        if (cs.done) break;
+        ++ref;
+        float act[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) act[r] = cs.active[r] ? 1.0f : 0.0f;
+        float rho[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) rho[r] = 0.0f;
+        for (int k = tid; k < nI; k += NT) {
+          const int g = interior(k);
+#pragma unroll
+          for (int r = 0; r < 8; ++r) {
+            const float rv = (float)r64[r * G + g] * act[r];
+            rr32[r * G + g] = rv;
+            pp32[r * G + g] = rv;
+            dd32[r * G + g] = 0.0f;
+            rho[r] = fmaf(rv, rv, rho[r]);
+          }
+        }
+        int buf = 0;
+        auto block_sum8 = [&](float (&v)[8]) {
+          float vv[8];
+#pragma unroll
+          for (int r = 0; r < 8; ++r) vv[r] = v[r];
+          const float t = warp_transpose_reduce<8>(vv, lane);
+          float *rb = reinterpret_cast<float *>(red[buf]);
+          if ((lane & 3) == 0) rb[warp * 8 + (lane >> 2)] = t;
+          __syncthreads();
+          float s = 0.f;
+          for (int i = lane; i < NW * 8; i += 32) s += rb[i];
+#pragma unroll
+          for (int mm = 8; mm < 32; mm <<= 1) s += shfl_xor_d(s, mm);
+#pragma unroll
+          for (int r = 0; r < 8; ++r) v[r] = __shfl_sync(0xffffffffu, s, r);
+          buf ^= 1;
+        };
+        block_sum8(rho);
+        float rho0[8];
+        bool iact[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+          rho0[r] = rho[r];
+          iact[r] = act[r] > 0.0f && rho[r] > 0.0f;
+        }
+        int iit = 0;
+        for (;;) {
+          bool any = false;
+#pragma unroll
+          for (int r = 0; r < 8; ++r) any |= iact[r];
+          if (!any || iit >= p.inner_maxit) break;
+          ++iit;
+          float sg[8];
+#pragma unroll
+          for (int r = 0; r < 8; ++r) sg[r] = 0.f;
+          for (int k = tid; k < nI; k += NT) {
+            const int g = interior(k);
+            float y[8];
+            stencil27<float>(c32, pp32, G, cs.offs, g, y);
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+              qq32[r * G + g] = y[r];
+              sg[r] = fmaf(pp32[r * G + g], y[r], sg[r]);
+            }
+          }
+          block_sum8(sg);
+          float al[8], rp[8];
+#pragma unroll
+          for (int r = 0; r < 8; ++r) {
+            al[r] = (iact[r] && sg[r] > 0.f) ? rho[r] / sg[r] : 0.0f;
+            rp[r] = 0.f;
+          }
+          for (int k = tid; k < nI; k += NT) {
+            const int g = interior(k);
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+              dd32[r * G + g] = fmaf(al[r], pp32[r * G + g], dd32[r * G + g]);
+              const float rv = fmaf(-al[r], qq32[r * G + g], rr32[r * G + g]);
+              rr32[r * G + g] = rv;
+              rp[r] = fmaf(rv, rv, rp[r]);
+            }
+          }
+          block_sum8(rp);
+          float be[8];
+#pragma unroll
+          for (int r = 0; r < 8; ++r) {
+            be[r] = 0.0f;
+            if (iact[r]) {
+              total_iters[r] += 1;
+              if (!(rp[r] <= itol2 * rho0[r]) && isfinite(rp[r])) {
+                be[r] = rp[r] / rho[r];
+                rho[r] = rp[r];
+              } else {
+                iact[r] = false;
+              }
+            }
+          }
+          for (int k = tid; k < nI; k += NT) {
+            const int g = interior(k);
+#pragma unroll
+            for (int r = 0; r < 8; ++r) pp32[r * G + g] = fmaf(be[r], pp32[r * G + g], rr32[r * G + g]);
+          }
+          __syncthreads();
+        }
+        // x~ += d (FP64); r = -(A~ phi~)_I in FP64
+        for (int k = tid; k < nI; k += NT) {
+          const int g = interior(k);
+#pragma unroll
+          for (int r = 0; r < 8; ++r) x64[r * G + g] += (double)dd32[r * G + g];
+        }
+        __syncthreads();
+        for (int k = tid; k < nI; k += NT) {
+          const int g = interior(k);
+          double y[8];
+          stencil27<double>(c64, x64, G, cs.offs, g, y);
+#pragma unroll
+          for (int r = 0; r < 8; ++r) r64[r * G + g] = -y[r];
+        }
+        __syncthreads();
+      }
+      if (tid == 0) cs.refinements = ref;
+      __syncthreads();
+    }
+
+    // ---------------- epilogue: M (64), F (8), true residual (8) -----------
+    // x64 holds phi~ (the boundary values were never overwritten)
+    const double fj = p.f_value;
+    for (int part = 0; part < 3; ++part) {
+      double acc[32];
+#pragma unroll
+      for (int i = 0; i < 32; ++i) acc[i] = 0.0;
+      for (int k = tid; k < nn; k += NT) {
+        const int ix = k % n, iy = (k / n) % n, iz = k / (n * n);
+        const int g = grid3(P, ix, iy, iz);
+        if (part < 2) {
+          double y[8];
+          stencil27<double>(c64, x64, G, cs.offs, g, y);
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const double ph = x64[(long)(4 * part + i) * G + g];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) acc[8 * i + j] = fma(ph, y[j], acc[8 * i + j]);
+          }
+        } else {
+          // load vector b_k (affine: f |det| / 8 per adjacent fine cell)
+          double bl;
+          if (cs.affine) {
+            const double mult = (ix == 0 || ix == N ? 1.0 : 2.0) * (iy == 0 || iy == N ? 1.0 : 2.0) *
+                                (iz == 0 || iz == N ? 1.0 : 2.0);
+            bl = fj * 0.125 * cs.absdet * mult;
+          } else {
+            const double invN = 1.0 / (double)N;
+            bl = 0.0;
+            for (int c8 = 0; c8 < 8; ++c8) {
+              const int cx = ix - (c8 & 1), cy = iy - ((c8 >> 1) & 1), cz = iz - (c8 >> 2);
+              if (cx < 0 || cy < 0 || cz < 0 || cx >= N || cy >= N || cz >= N) continue;
+              const int kv = (c8 & 1) + 2 * ((c8 >> 1) & 1) + 4 * (c8 >> 2);  // local vertex
+              double V[24];
+              for (int k8 = 0; k8 < 8; ++k8) {
+                const double t[3] = {(cx + (k8 & 1)) * invN, (cy + ((k8 >> 1) & 1)) * invN, (cz + (k8 >> 2)) * invN};
+                trilinear_map(cs.corners, t, V + 3 * k8);
+              }
+              for (int q = 0; q < 8; ++q) {
+                double J[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+                for (int k8 = 0; k8 < 8; ++k8)
+                  for (int a = 0; a < 3; ++a)
+                    for (int c = 0; c < 3; ++c) J[3 * a + c] += V[3 * k8 + a] * rgrad(k8, q, c);
+                const double det = J[0] * (J[4] * J[8] - J[5] * J[7]) + J[1] * (J[5] * J[6] - J[3] * J[8]) +
+                                   J[2] * (J[3] * J[7] - J[4] * J[6]);
+                const double psi = lv3(kv & 1, q & 1) * lv3((kv >> 1) & 1, (q >> 1) & 1) * lv3(kv >> 2, q >> 2);
+                bl += psi * 0.125 * fabs(det);
+              }
+            }
+            bl *= fj;
+          }
+          const double d = d64[g];
+          const double s = rsqrt(d);
+#pragma unroll
+          for (int i = 0; i < 8; ++i) acc[i] = fma(x64[(long)i * G + g], bl * s, acc[i]);
+          if (ix > 0 && iy > 0 && iz > 0 && ix < N && iy < N && iz < N) {
+            double y[8];
+            stencil27<double>(c64, x64, G, cs.offs, g, y);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) acc[8 + j] = fma(y[j] * d, y[j], acc[8 + j]);
+          }
+          if (p.basis) {
+            double *out = p.basis + (p.basis_offset ? p.basis_offset[cell] : (int64_t)cell * 8 * nn);
+#pragma unroll
+            for (int i = 0; i < 8; ++i) out[(int64_t)i * nn + k] = x64[(long)i * G + g] * s;
+          }
+        }
+      }
+      const double tot = warp_transpose_reduce<32>(acc, lane);
+      redE[warp * 32 + lane] = tot;
+      __syncthreads();
+      if (warp == 0) {
+        double s = 0.0;
+        for (int w = 0; w < NW; ++w) s += redE[w * 32 + lane];
+        if (part < 2) {
+          p.M[(int64_t)cell * 64 + part * 32 + lane] = s;
+        } else {
+          if (lane < 8) p.F[(int64_t)cell * 8 + lane] = s;
+          double rel = 0.0;
+          if (lane >= 8 && lane < 16) {
+            const double bb = cs.bb[lane - 8];
+            const double nu = MIXED ? cs.nu[lane - 8] : s;
+            rel = bb > 0.0 ? sqrt(nu / bb) : sqrt(nu);
+          }
+#pragma unroll
+          for (int mm = 16; mm >= 1; mm >>= 1) rel = fmax(rel, shfl_xor_d(rel, mm));
+          if (lane < 8 && p.iters) {
+            const int itv = cs.iters[lane];
+            p.iters[(int64_t)cell * 8 + lane] =
+                MIXED ? total_iters[lane] : (itv >= 0 ? itv : (itv <= -1000000 ? -itv - 1000000 : -itv));
+          }
+          if (lane == 0) {
+            int st = cs.status;
+            for (int r = 0; r < 8; ++r) {
+              const int itv = cs.iters[r];
+              if (itv <= -1000000) st = st == MSFEM_CELL_CONVERGED ? MSFEM_CELL_MAXIT : st;
+              else if (itv < 0) st = MSFEM_CELL_NAN;
+            }
+            if (!isfinite(rel)) st = MSFEM_CELL_NAN;
+            p.status[cell] = st;
+            if (p.rel_res) p.rel_res[cell] = rel;
+            if (p.refinements) p.refinements[cell] = cs.refinements;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
 }
 
 }  // namespace msfem

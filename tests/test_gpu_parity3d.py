@@ -1,0 +1,81 @@
+"""3D GPU parity against the CPU FP64 oracle: trilinear Q1 assembly, 8
+Dirichlet solves per cell, coarse 8x8 matrix and load.  Same tolerances as 2D:
+M, F within 1e-10 relative, basis values within 1e-9 absolute."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL_REL = 1e-10
+
+
+def rel_err(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def check(got, ref, basis=True):
+    assert got["rc"] == 0, got["status"]
+    assert np.all(got["status"] == 0)
+    assert rel_err(got["M"], ref["M"]) < TOL_REL
+    assert rel_err(got["F"], ref["F"]) < TOL_REL
+    if basis:
+        assert np.abs(got["basis"] - ref["basis"]).max() < 1e-9
+
+
+def test_constant_diagonal_tensor_kat_3d(pkg, engine):
+    W = pkg.workloads
+    a = (2.0, 0.5, 1.5)
+    prob = W.problem(3, W.unit_cube_corners(3, 2), 6, {"kind": 0, "params": [a[0], 0, 0, a[1], 0, a[2]]},
+                     f_value=3.0)
+    got = engine.run(prob, precision="fp64", tol=1e-13)
+    H = 0.5
+    K1 = np.array([[1.0, -1.0], [-1.0, 1.0]]) / H
+    M1 = np.array([[2.0, 1.0], [1.0, 2.0]]) * H / 6.0
+    exact = (a[0] * np.kron(M1, np.kron(M1, K1)) + a[1] * np.kron(M1, np.kron(K1, M1))
+             + a[2] * np.kron(K1, np.kron(M1, M1)))
+    assert np.abs(got["M"] - exact).max() < 1e-11
+    assert np.allclose(got["F"], 3.0 * H ** 3 / 8, rtol=1e-12)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_reference_coefficient_3d(pkg, oracle, engine, precision):
+    """The reference MatrixCoeff<3> (ZXZ Euler rotation, PI_D) on a 2^3 coarse mesh."""
+    prob = pkg.workloads.reference_problem(3, 1, 3)  # 8 coarse cells, N = 8
+    got = engine.run(prob, precision=precision, tol=1e-13, want_basis=True)
+    ref = oracle.run(prob, want_basis=True)
+    check(got, ref)
+
+
+@pytest.mark.parametrize("N", [1, 2, 3, 5])
+def test_ragged_sizes_3d(pkg, oracle, engine, N):
+    W = pkg.workloads
+    prob = W.problem(3, W.unit_cube_corners(3, 2), N, {"kind": 2, "params": [0.5, 0.5]})
+    got = engine.run(prob, precision="fp64", tol=1e-13, want_basis=True)
+    ref = oracle.run(prob, want_basis=True)
+    check(got, ref)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_spheres_uneven_one_launch(pkg, oracle, engine, precision):
+    """Config-4 coefficient (1e4-contrast spheres) with uneven N in one launch."""
+    W = pkg.workloads
+    rng = np.random.default_rng(5)
+    sp = np.column_stack([rng.uniform(0, 1, (600, 3)), rng.uniform(0.02, 0.05, 600)])
+    corners = W.unit_cube_corners(3, 4)[[0, 5, 21, 42, 63]]
+    nf = np.array([8, 4, 12, 6, 8], dtype=np.int32)
+    prob = W.problem(3, corners, nf, {"kind": 4, "params": [1e4], "spheres": sp})
+    got = engine.run(prob, precision=precision, tol=1e-12, want_basis=True)
+    ref = oracle.run(prob, want_basis=True)
+    assert got["stats"]["kernel_launches"] == 2  # tabulation + one basis kernel
+    assert got["rc"] == 0 and np.all(got["status"] == 0)
+    assert rel_err(got["M"], ref["M"]) < 1e-9
+    assert rel_err(got["F"], ref["F"]) < TOL_REL
+    assert np.abs(got["basis"] - ref["basis"]).max() < 1e-8
+
+
+def test_fp64_iterations_match_oracle_jacobi_pcg_3d(pkg, oracle, engine):
+    W = pkg.workloads
+    prob = W.problem(3, W.unit_cube_corners(3, 2), 6, {"kind": 2, "params": [0.8, 0.25]})
+    got = engine.run(prob, precision="fp64", tol=1e-10, check_interval=1)
+    ref = oracle.run(prob, solver=oracle.SOLVER_JACOBI_CG, tol=1e-10)
+    assert np.abs(got["iters"] - ref["iters"]).max() <= 2
