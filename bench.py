@@ -203,6 +203,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 timing (profiling runs)")
+    ap.add_argument("--no-config3", action="store_true", help="skip the 65536-cell config-3 timing")
     ap.add_argument("--coarse", type=int, default=K_COARSE, help="coarse cells per direction")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -228,51 +229,6 @@ def main():
     torch.cuda.set_stream(stream)
     eng.set_stream(stream.cuda_stream)
 
-    # ---- workload on the device: corners + tabulated coefficient (weak scaling:
-    # every rank owns its own 64x64 block of coarse cells)
-    prob = W.config2(K=args.coarse, N=N_FINE)
-    corners_h = prob["corners"] + np.array([float(rank), 0.0])
-    n_cells = corners_h.shape[0]
-    solves_rank = 4 * n_cells
-    corners_d = torch.from_numpy(np.ascontiguousarray(corners_h)).to(f"cuda:{local}")
-    modes = np.ascontiguousarray(prob["coef"]["modes"])
-    dtab = abi.BatchDesc()
-    dtab.dim, dtab.n_cells, dtab.n_fine = 2, n_cells, N_FINE
-    dtab.corners = corners_d.data_ptr()
-    dtab.coef.kind = abi.COEF_FOURIER
-    dtab.coef.modes = modes.ctypes.data  # mode table: host memory is accepted for tabulation input
-    dtab.coef.n_modes = modes.shape[1]
-    dtab.memory = abi.MEM_HOST
-    dtab.tol, dtab.maxit = TOL, 1000
-    size = eng.lib.msfem_tabulated_size(ctypes.byref(dtab), 3)
-    tab_d = torch.empty(size, dtype=torch.float64, device=f"cuda:{local}")
-    # tabulate on the host-memory path into a host buffer is slow for 400 MB; use
-    # the device path: device corners + device mode table
-    modes_d = torch.from_numpy(modes).to(f"cuda:{local}")
-    dtab.coef.modes = modes_d.data_ptr()
-    dtab.memory = abi.MEM_DEVICE
-    rc = eng.lib.msfem_tabulate_coefficient(eng.handle, ctypes.byref(dtab), 3, tab_d.data_ptr())
-    if rc != abi.OK:
-        raise abi.MsfemError(rc, abi.last_error(eng.lib))
-
-    def device_desc(precision):
-        d = abi.BatchDesc()
-        d.dim, d.n_cells, d.n_fine = 2, n_cells, N_FINE
-        d.precision = precision
-        d.corners = corners_d.data_ptr()
-        d.coef.kind = abi.COEF_TABULATED
-        d.coef.ncomp = 3
-        d.coef.qp_values = tab_d.data_ptr()
-        d.f_value = 1.0
-        d.tol, d.maxit = TOL, 1000
-        d.memory = abi.MEM_DEVICE
-        return d
-
-    M_d = torch.empty((n_cells, 4, 4), dtype=torch.float64, device=f"cuda:{local}")
-    F_d = torch.empty((n_cells, 4), dtype=torch.float64, device=f"cuda:{local}")
-    st_d = torch.empty(n_cells, dtype=torch.int32, device=f"cuda:{local}")
-    it_d = torch.empty((n_cells, 4), dtype=torch.int32, device=f"cuda:{local}")
-
     def barrier():
         if world > 1:
             torch.distributed.barrier()
@@ -284,9 +240,49 @@ def main():
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         return float(t.item())
 
-    def timed(precision, steps, warmup, sample_clocks=False):
-        d = device_desc(precision)
-        args_ = (M_d.data_ptr(), F_d.data_ptr(), None, st_d.data_ptr(), it_d.data_ptr())
+    def make_ws(prob, shift):
+        """Device workload: corners + the coefficient tabulated at the Gauss
+        points (input data, tabulated once by the library's field kernel)."""
+        corners_h = np.ascontiguousarray(prob["corners"] + np.array([float(shift), 0.0]))
+        n = corners_h.shape[0]
+        corners_d = torch.from_numpy(corners_h).to(f"cuda:{local}")
+        modes_d = torch.from_numpy(np.ascontiguousarray(prob["coef"]["modes"])).to(f"cuda:{local}")
+        dt = abi.BatchDesc()
+        dt.dim, dt.n_cells, dt.n_fine = 2, n, N_FINE
+        dt.corners = corners_d.data_ptr()
+        dt.coef.kind = abi.COEF_FOURIER
+        dt.coef.modes = modes_d.data_ptr()
+        dt.coef.n_modes = modes_d.shape[1]
+        dt.memory = abi.MEM_DEVICE
+        dt.tol, dt.maxit = TOL, 1000
+        size = eng.lib.msfem_tabulated_size(ctypes.byref(dt), 3)
+        tab_d = torch.empty(size, dtype=torch.float64, device=f"cuda:{local}")
+        rc = eng.lib.msfem_tabulate_coefficient(eng.handle, ctypes.byref(dt), 3, tab_d.data_ptr())
+        if rc != abi.OK:
+            raise abi.MsfemError(rc, abi.last_error(eng.lib))
+        ws = {"n": n, "corners_h": corners_h, "corners_d": corners_d, "tab_d": tab_d, "size": size,
+              "M": torch.empty((n, 4, 4), dtype=torch.float64, device=f"cuda:{local}"),
+              "F": torch.empty((n, 4), dtype=torch.float64, device=f"cuda:{local}"),
+              "st": torch.empty(n, dtype=torch.int32, device=f"cuda:{local}"),
+              "it": torch.empty((n, 4), dtype=torch.int32, device=f"cuda:{local}")}
+        return ws
+
+    def device_desc(ws, precision):
+        d = abi.BatchDesc()
+        d.dim, d.n_cells, d.n_fine = 2, ws["n"], N_FINE
+        d.precision = precision
+        d.corners = ws["corners_d"].data_ptr()
+        d.coef.kind = abi.COEF_TABULATED
+        d.coef.ncomp = 3
+        d.coef.qp_values = ws["tab_d"].data_ptr()
+        d.f_value = 1.0
+        d.tol, d.maxit = TOL, 1000
+        d.memory = abi.MEM_DEVICE
+        return d
+
+    def timed_ws(ws, precision, steps, warmup, sample_clocks=False):
+        d = device_desc(ws, precision)
+        args_ = (ws["M"].data_ptr(), ws["F"].data_ptr(), None, ws["st"].data_ptr(), ws["it"].data_ptr())
         for _ in range(warmup):
             eng.run_desc(d, *args_, stats=False)
         torch.cuda.synchronize()
@@ -306,6 +302,17 @@ def main():
         # correctness / work accounting of the same workload (untimed)
         _, st = eng.run_desc(d, *args_, stats=True)
         return max_over_ranks(ms), st, clocks
+
+    # ---- workload on the device (weak scaling: every rank owns its own
+    # 64x64 block of coarse cells, shifted by the rank along x)
+    prob = W.config2(K=args.coarse, N=N_FINE)
+    ws2 = make_ws(prob, rank)
+    n_cells, size, corners_h = ws2["n"], ws2["size"], ws2["corners_h"]
+    solves_rank = 4 * n_cells
+    M_d, F_d = ws2["M"], ws2["F"]
+
+    def timed(precision, steps, warmup, sample_clocks=False):
+        return timed_ws(ws2, precision, steps, warmup, sample_clocks)
 
     # ---- FP64 form (headline)
     if args.no_fp64:
@@ -378,7 +385,7 @@ def main():
         M_h = torch.empty((n_cells, 4, 4), dtype=torch.float64, pin_memory=True)
         F_h = torch.empty((n_cells, 4), dtype=torch.float64, pin_memory=True)
         st_h = torch.empty(n_cells, dtype=torch.int32, pin_memory=True)
-        d = device_desc(abi.PREC_FP64)
+        d = device_desc(ws2, abi.PREC_FP64)
         d.memory = abi.MEM_HOST
         d.corners = corners_pin.data_ptr()
         d.coef.qp_values = tab_h.data_ptr()
@@ -398,6 +405,28 @@ def main():
                        "d2h_bytes_per_step": int(M_h.numel() * 8 + F_h.numel() * 8 + st_h.numel() * 4)}
         # sanity: host result equals the device-resident one
         line["e2e"]["matches_device"] = bool(np.array_equal(M_h.numpy(), M64))
+    # ---- config 3 workload: 256x256 coarse cells (65536), mixed vs FP64
+    if not args.no_config3 and world == 1 and args.coarse == K_COARSE:
+        ws3 = make_ws(W.config3(), 0)
+        st3 = max(2, min(5, args.steps))
+        ms3m, s3m, _ = timed_ws(ws3, abi.PREC_MIXED, st3, 3)
+        ms3f, s3f, _ = timed_ws(ws3, abi.PREC_FP64, 2, 3)
+        n3 = ws3["n"]
+        line["config3"] = {
+            "workload": "2D 256x256 coarse cells, 32x32 fine Q1, 4 RHS, random-Fourier SPD tensor "
+                        "(seeds 3/30/300), f=1, 1e-10 rel residual",
+            "mixed": {"value": 4 * n3 / (ms3m * 1e-3), "unit": UNIT, "ms_per_step": ms3m,
+                      "mean_inner_iterations": s3m["iterations_total"] / max(1, s3m["solves"]),
+                      "max_refinements": s3m["refinements_max"],
+                      "max_rel_residual": s3m["max_rel_residual"], "cells_failed": s3m["cells_failed"]},
+            "fp64": {"value": 4 * n3 / (ms3f * 1e-3), "unit": UNIT, "ms_per_step": ms3f,
+                     "mean_iterations": s3f["iterations_total"] / max(1, s3f["solves"]),
+                     "max_rel_residual": s3f["max_rel_residual"], "cells_failed": s3f["cells_failed"]},
+            "speedup_mixed_vs_fp64": ms3f / ms3m,
+        }
+        line["gpu_launches_config3"] = st3 + 2
+        del ws3
+        torch.cuda.empty_cache()
     # ---- CPU baseline (rank 0, N = 1 only)
     if rank == 0 and world == 1 and not args.no_cpu:
         oracle = graft.load_oracle()

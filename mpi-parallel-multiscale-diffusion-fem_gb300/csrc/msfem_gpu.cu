@@ -80,6 +80,11 @@ struct msfem_handle {
   // outputs staged to the host / internal
   DevBuf M, F, basis, status, iters, relres, refine;
   DevBuf work;  // per-CTA workspace slots of the 3D kernels
+  // CUDA graph of the last device-resident launch sequence
+  bool use_graphs = true;
+  std::string graph_key;
+  cudaGraphExec_t graph_exec = nullptr;
+  int64_t graph_launches = 0;
   // autotuned launch choices, keyed by (dim, N class, precision)
   std::map<int, Tune> tuning;
 };
@@ -649,6 +654,7 @@ int msfem_destroy(msfem_handle *h) {
                     &h->M, &h->F, &h->basis, &h->status, &h->iters, &h->relres, &h->refine,
                     &h->work};
   for (DevBuf *b : bufs) b->release();
+  if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
@@ -902,13 +908,56 @@ int run_batch_impl(msfem_handle *h, const msfem_batch_desc *d, double *M, double
     MSFEM_CUDA(h->work.ensure(slot_bytes * grid));
     work = h->work.as<unsigned char>();
   }
-  MSFEM_CUDA(cudaMemsetAsync(p.queue, 0, sizeof(unsigned int), h->stream));
+  // Device-resident asynchronous calls replay a CUDA graph of the
+  // queue-reset + basis-kernel sequence; it is re-captured whenever the
+  // launch parameters (pointers, sizes, tuning) change.
+  const bool graph_ok = dev && !stats && nc > 0 && h->use_graphs && h->stream != nullptr &&
+                        h->stream != cudaStreamLegacy && h->stream != cudaStreamPerThread;
   MSFEM_CUDA(cudaEventRecord(h->ev0, h->stream));
-  if (nc > 0) {
-    void *args2[] = {&p};
-    void *args3[] = {&p, &work, &slot_bytes};
-    MSFEM_CUDA(cudaLaunchKernel(L.fn, dim3(grid), dim3(L.nt), slot_bytes ? args3 : args2, L.smem, h->stream));
+  if (graph_ok) {
+    std::string key(reinterpret_cast<const char *>(&p), sizeof(p));
+    key.append(reinterpret_cast<const char *>(&L.fn), sizeof(L.fn));
+    key.append(reinterpret_cast<const char *>(&L.nt), sizeof(L.nt));
+    key.append(reinterpret_cast<const char *>(&L.smem), sizeof(L.smem));
+    key.append(reinterpret_cast<const char *>(&slot_bytes), sizeof(slot_bytes));
+    key.append(reinterpret_cast<const char *>(&grid), sizeof(grid));
+    key.append(reinterpret_cast<const char *>(&work), sizeof(work));
+    key.append(reinterpret_cast<const char *>(&h->stream), sizeof(h->stream));
+    if (key != h->graph_key || !h->graph_exec) {
+      if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+      h->graph_exec = nullptr;
+      h->graph_key.clear();
+      cudaGraph_t graph = nullptr;
+      MSFEM_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+      cudaError_t e1 = cudaMemsetAsync(p.queue, 0, sizeof(unsigned int), h->stream);
+      void *a2[] = {&p};
+      void *a3[] = {&p, &work, &slot_bytes};
+      cudaError_t e2 = cudaLaunchKernel(L.fn, dim3(grid), dim3(L.nt), slot_bytes ? a3 : a2, L.smem, h->stream);
+      cudaError_t e3 = cudaStreamEndCapture(h->stream, &graph);
+      if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return fail(MSFEM_ERR_CUDA, std::string("graph capture failed: ") +
+                                        cudaGetErrorString(e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : e3)));
+      }
+      const cudaError_t e4 = cudaGraphInstantiate(&h->graph_exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (e4 != cudaSuccess) {
+        h->graph_exec = nullptr;
+        return fail(MSFEM_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e4));
+      }
+      h->graph_key = key;
+    }
+    MSFEM_CUDA(cudaGraphLaunch(h->graph_exec, h->stream));
     launches++;
+    h->graph_launches++;
+  } else {
+    MSFEM_CUDA(cudaMemsetAsync(p.queue, 0, sizeof(unsigned int), h->stream));
+    if (nc > 0) {
+      void *args2[] = {&p};
+      void *args3[] = {&p, &work, &slot_bytes};
+      MSFEM_CUDA(cudaLaunchKernel(L.fn, dim3(grid), dim3(L.nt), slot_bytes ? args3 : args2, L.smem, h->stream));
+      launches++;
+    }
   }
   MSFEM_CUDA(cudaEventRecord(h->ev1, h->stream));
 
