@@ -380,7 +380,7 @@ def main():
     # ---- e2e through the public C-ABI with pinned host buffers
     if not args.no_e2e:
         tab_h = torch.empty(size, dtype=torch.float64, pin_memory=True)
-        tab_h.copy_(tab_d.cpu())
+        tab_h.copy_(ws2["tab_d"].cpu())
         corners_pin = torch.from_numpy(np.ascontiguousarray(corners_h)).pin_memory()
         M_h = torch.empty((n_cells, 4, 4), dtype=torch.float64, pin_memory=True)
         F_h = torch.empty((n_cells, 4), dtype=torch.float64, pin_memory=True)
