@@ -122,7 +122,8 @@ typedef enum msfem_memory {
 
 typedef enum msfem_warm_start {
   MSFEM_WARM_NONE = 0,          /* x0 = 0 in the interior (reference behaviour) */
-  MSFEM_WARM_USER = 1           /* x0 = warm_basis (interior values used) */
+  MSFEM_WARM_USER = 1,          /* x0 = warm_basis (interior values used) */
+  MSFEM_WARM_SURROGATE = 2      /* x0 = prediction of the surrogate attached to the handle */
 } msfem_warm_start;
 
 typedef struct msfem_coef_desc {
@@ -272,6 +273,52 @@ int64_t msfem_tabulated_size(const msfem_batch_desc *desc, int32_t ncomp);
 int msfem_run_batch_noalloc(const msfem_batch_desc *desc, double *M, double *F,
                             double *basis, int32_t *cell_status,
                             int32_t *iterations, void *stream);
+
+/* ---------------------------------------------------------------------------
+ * Learned warm start (no counterpart in the reference): a 6-layer 3x3
+ * convolutional network, 3 -> 32 -> 32 -> 32 -> 32 -> 32 -> 4 channels, that
+ * maps a 2D cell's coefficient on its 33 x 33 fine nodal grid (N = 32) to the
+ * corrections delta_i = phi_i - Q1_i of the four basis functions.  BF16
+ * weights and activations with FP32 accumulation on the tensor cores, FP32
+ * master weights, Adam.  The CG always runs to the requested tolerance from
+ * the predicted start, so the network only changes the iteration count.
+ *   features  [n][3][33][33] FP32: log a11, a12/sqrt(a11 a22), log a22 at the nodes
+ *   targets / predictions [n][4][33][33] FP32 (delta_i, zero on the boundary)
+ *   parameters: FP32, per layer W [Cout][Cin][3][3] then b [Cout]
+ * All feature / target / prediction pointers are device pointers.
+ * ------------------------------------------------------------------------- */
+typedef struct msfem_surrogate msfem_surrogate;
+
+int64_t msfem_surrogate_param_count(void);
+
+/* New network on the handle's device and stream, seeded uniform init. */
+int msfem_surrogate_create(msfem_handle *handle, uint64_t seed, msfem_surrogate **net);
+int msfem_surrogate_destroy(msfem_surrogate *net);
+int msfem_surrogate_set_params(msfem_surrogate *net, const float *params_host);
+int msfem_surrogate_get_params(msfem_surrogate *net, float *params_host);
+
+/* Node features of a 2D, N = 32 batch whose coefficient is TABULATED in
+ * device memory (desc->memory == MSFEM_MEM_DEVICE). */
+int msfem_surrogate_features(msfem_handle *handle, const msfem_batch_desc *desc, float *features);
+
+/* Training targets from computed basis functions: delta_i = phi_i - Q1_i at
+ * the nodes, basis [n][4][33*33] FP64 -> delta [n][4][33][33] FP32. */
+int msfem_surrogate_targets(msfem_handle *handle, const double *basis, int32_t n, float *delta);
+
+/* Forward pass: predictions for n cells. */
+int msfem_surrogate_predict(msfem_surrogate *net, const float *features, int32_t n, float *delta);
+
+/* Loss (mean squared error over interior nodes) and parameter gradients
+ * (host FP32, msfem_surrogate_param_count values) without updating. */
+int msfem_surrogate_gradients(msfem_surrogate *net, const float *features, const float *targets,
+                              int32_t batch, float *grads_host, double *loss);
+
+/* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8) on a batch. */
+int msfem_surrogate_train_step(msfem_surrogate *net, const float *features, const float *targets,
+                               int32_t batch, float lr, double *loss);
+
+/* The network used by MSFEM_WARM_SURROGATE on this handle (NULL detaches). */
+int msfem_attach_surrogate(msfem_handle *handle, msfem_surrogate *net);
 
 /* Message of the last failing call on this thread. */
 int msfem_last_error(char *buf, size_t len);

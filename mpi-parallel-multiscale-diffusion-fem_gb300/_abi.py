@@ -40,6 +40,7 @@ MEM_HOST = 0
 MEM_DEVICE = 1
 WARM_NONE = 0
 WARM_USER = 1
+WARM_SURROGATE = 2
 
 MAX_N_2D = 32
 MAX_N_3D = 24
@@ -141,6 +142,25 @@ EXPORTS = {
     "msfem_run_batch_noalloc": (ctypes.c_int, [ctypes.POINTER(BatchDesc), ctypes.c_void_p,
                                                ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                ctypes.c_void_p, ctypes.c_void_p]),
+    "msfem_surrogate_param_count": (ctypes.c_int64, []),
+    "msfem_surrogate_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64,
+                                              ctypes.POINTER(ctypes.c_void_p)]),
+    "msfem_surrogate_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "msfem_surrogate_set_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "msfem_surrogate_get_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "msfem_surrogate_features": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BatchDesc),
+                                                ctypes.c_void_p]),
+    "msfem_surrogate_targets": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                                               ctypes.c_void_p]),
+    "msfem_surrogate_predict": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                                               ctypes.c_void_p]),
+    "msfem_surrogate_gradients": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                 ctypes.c_int32, ctypes.c_void_p,
+                                                 ctypes.POINTER(ctypes.c_double)]),
+    "msfem_surrogate_train_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                  ctypes.c_int32, ctypes.c_float,
+                                                  ctypes.POINTER(ctypes.c_double)]),
+    "msfem_attach_surrogate": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "msfem_last_error": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
     "msfem_version": (ctypes.c_char_p, []),
 }

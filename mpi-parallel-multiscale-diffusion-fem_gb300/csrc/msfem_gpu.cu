@@ -20,6 +20,7 @@
 #include "msfem_common.cuh"
 #include "msfem_kernel2d.cuh"
 #include "msfem_kernel3d.cuh"
+#include "msfem_cnn.cuh"
 #include "msfem_gpu.h"
 
 namespace {
@@ -80,6 +81,9 @@ struct msfem_handle {
   // outputs staged to the host / internal
   DevBuf M, F, basis, status, iters, relres, refine;
   DevBuf work;  // per-CTA workspace slots of the 3D kernels
+  // learned warm start
+  msfem_surrogate *surrogate = nullptr;
+  DevBuf feat, delta, warm_pred;
   // CUDA graph of the last device-resident launch sequence
   bool use_graphs = true;
   std::string graph_key;
@@ -392,7 +396,8 @@ int validate(const msfem_batch_desc *d) {
   if (!(d->tol > 0.0) || !std::isfinite(d->tol)) return fail(MSFEM_ERR_INVALID_ARG, "tol must be > 0");
   if (d->maxit < 1) return fail(MSFEM_ERR_INVALID_ARG, "maxit must be >= 1");
   if (d->check_interval < 0) return fail(MSFEM_ERR_INVALID_ARG, "check_interval < 0");
-  if (d->warm_start != MSFEM_WARM_NONE && d->warm_start != MSFEM_WARM_USER)
+  if (d->warm_start != MSFEM_WARM_NONE && d->warm_start != MSFEM_WARM_USER &&
+      d->warm_start != MSFEM_WARM_SURROGATE)
     return fail(MSFEM_ERR_INVALID_ARG, "unknown warm_start");
   if (d->warm_start == MSFEM_WARM_USER && d->n_cells > 0 && !d->warm_basis)
     return fail(MSFEM_ERR_INVALID_ARG, "warm_basis is NULL");
@@ -726,6 +731,376 @@ int msfem_tabulate_coefficient(msfem_handle *h, const msfem_batch_desc *d, int32
 
 }  // extern "C"
 
+// ===========================================================================
+// Learned warm start: network object, training and inference
+// ===========================================================================
+namespace msfem {
+
+// Node features of N = 32 cells from the tabulated coefficient:
+// the tensor averaged over the node's fine cells (4 Gauss points each),
+// then (log a11, a12 / sqrt(a11 a22), log a22).
+__global__ void features_kernel(const double *__restrict__ qp, int ncomp, const int64_t *__restrict__ qp_offset,
+                                int n_cells, float *__restrict__ feat) {
+  constexpr int N = 32, n = 33, nfc = N * N;
+  const int cell = blockIdx.x;
+  if (cell >= n_cells) return;
+  const double *tab = qp + (qp_offset ? qp_offset[cell] : (int64_t)cell * ncomp * 4 * nfc);
+  for (int k = threadIdx.x; k < n * n; k += blockDim.x) {
+    const int ix = k % n, iy = k / n;
+    double a[3] = {0.0, 0.0, 0.0};
+    int cnt = 0;
+    for (int dy = -1; dy <= 0; ++dy)
+      for (int dx = -1; dx <= 0; ++dx) {
+        const int cx = ix + dx, cy = iy + dy;
+        if (cx < 0 || cy < 0 || cx >= N || cy >= N) continue;
+        const int fc = cx + N * cy;
+        ++cnt;
+        for (int q = 0; q < 4; ++q) {
+          if (ncomp == 1) {
+            const double v = __ldg(tab + (int64_t)q * nfc + fc);
+            a[0] += v;
+            a[2] += v;
+          } else {
+            for (int c = 0; c < 3; ++c) a[c] += __ldg(tab + ((int64_t)c * 4 + q) * nfc + fc);
+          }
+        }
+      }
+    const double sc = 1.0 / (4.0 * cnt);
+    const double a11 = a[0] * sc, a12 = a[1] * sc, a22 = a[2] * sc;
+    float *o = feat + (int64_t)cell * 3 * n * n + k;
+    o[0] = (float)log(a11);
+    o[n * n] = (float)(a12 / sqrt(a11 * a22));
+    o[2 * n * n] = (float)log(a22);
+  }
+}
+
+// Warm basis = Q1 hat + predicted correction, FP64 [cell][4][33*33].
+__global__ void compose_warm_kernel(const float *__restrict__ delta, int n_cells, double *__restrict__ warm) {
+  constexpr int n = 33, nn = n * n;
+  const long total = (long)n_cells * 4 * nn;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+    const int k = (int)(i % nn), b = (int)((i / nn) % 4);
+    const double tx = (k % n) / 32.0, ty = (k / n) / 32.0;
+    const double hx = (b & 1) ? tx : 1.0 - tx, hy = (b & 2) ? ty : 1.0 - ty;
+    warm[i] = hx * hy + (double)delta[i];
+  }
+}
+
+// Training targets delta = phi - Q1 hat (inverse of compose_warm_kernel).
+__global__ void targets_kernel(const double *__restrict__ basis, int n_cells, float *__restrict__ delta) {
+  constexpr int n = 33, nn = n * n;
+  const long total = (long)n_cells * 4 * nn;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+    const int k = (int)(i % nn), b = (int)((i / nn) % 4);
+    const double tx = (k % n) / 32.0, ty = (k / n) / 32.0;
+    const double hx = (b & 1) ? tx : 1.0 - tx, hy = (b & 2) ? ty : 1.0 - ty;
+    delta[i] = (float)(basis[i] - hx * hy);
+  }
+}
+
+}  // namespace msfem
+
+struct msfem_surrogate {
+  msfem_handle *h = nullptr;
+  int capacity = 0;
+  int64_t step = 0;
+  DevBuf params, grads, m, v, loss;
+  DevBuf wf[msfem::cnn::kLayers], wt[msfem::cnn::kLayers], bpad[msfem::cnn::kLayers];
+  DevBuf act[msfem::cnn::kLayers + 1];  // act[0] input, act[1..5] hidden, act[6] FP32 prediction
+  DevBuf ga, gb;                        // gradient ping-pong (NHWC bf16)
+};
+
+namespace {
+
+using bf16 = __nv_bfloat16;
+namespace cn = msfem::cnn;
+
+template <int CIN, int COUT, int EPI>
+int launch_conv(cudaStream_t st, int B, const bf16 *X, const bf16 *W, const float *bias, const bf16 *mask,
+                void *out, int cout_real) {
+  const size_t smem = cn::conv_smem<CIN, COUT>();
+  auto fn = cn::conv3x3_kernel<CIN, COUT, EPI>;
+  MSFEM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  fn<<<B, 256, smem, st>>>(X, W, bias, mask, out, cout_real);
+  MSFEM_CUDA(cudaGetLastError());
+  return MSFEM_OK;
+}
+
+template <int XC, int GC>
+int launch_wgrad(cudaStream_t st, int sms, int B, const bf16 *X, const bf16 *G, int cin_real, int cout_real,
+                 float *dW, float *db) {
+  const size_t smem = cn::wgrad_smem<XC, GC>();
+  auto fn = cn::conv3x3_wgrad_kernel<XC, GC>;
+  MSFEM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  fn<<<std::max(1, std::min(B, sms)), 256, smem, st>>>(X, G, B, cin_real, cout_real, dW, db);
+  MSFEM_CUDA(cudaGetLastError());
+  return MSFEM_OK;
+}
+
+int surrogate_reserve(msfem_surrogate *s, int B) {
+  if (B <= s->capacity) return MSFEM_OK;
+  for (int l = 0; l < cn::kLayers; ++l)
+    MSFEM_CUDA(s->act[l].ensure(sizeof(bf16) * (size_t)B * cn::kPix * cn::pad_ch(l)));
+  MSFEM_CUDA(s->act[cn::kLayers].ensure(sizeof(float) * (size_t)B * 4 * cn::kPix));
+  MSFEM_CUDA(s->ga.ensure(sizeof(bf16) * (size_t)B * cn::kPix * 32));
+  MSFEM_CUDA(s->gb.ensure(sizeof(bf16) * (size_t)B * cn::kPix * 32));
+  s->capacity = B;
+  return MSFEM_OK;
+}
+
+int surrogate_pack(msfem_surrogate *s) {
+  cudaStream_t st = s->h->stream;
+  for (int l = 0; l < cn::kLayers; ++l) {
+    const size_t nw = (size_t)cn::pad_ch(l + 1) * 9 * cn::pad_ch(l);
+    MSFEM_CUDA(s->wf[l].ensure(sizeof(bf16) * nw));
+    MSFEM_CUDA(s->wt[l].ensure(sizeof(bf16) * nw));
+    MSFEM_CUDA(s->bpad[l].ensure(sizeof(float) * cn::pad_ch(l + 1)));
+    cn::pack_layer_kernel<<<64, 256, 0, st>>>(s->params.as<float>(), l, s->wf[l].as<bf16>(), s->wt[l].as<bf16>(),
+                                              s->bpad[l].as<float>());
+    MSFEM_CUDA(cudaGetLastError());
+  }
+  return MSFEM_OK;
+}
+
+// Forward pass of B images; the prediction goes to `out` (FP32 NCHW, 4 ch).
+int surrogate_forward(msfem_surrogate *s, const float *features, int B, float *out) {
+  cudaStream_t st = s->h->stream;
+  int rc;
+  if ((rc = surrogate_reserve(s, B))) return rc;
+  cn::features_to_nhwc_kernel<<<std::max(1, std::min(B * 4, 4096)), 256, 0, st>>>(features, B, s->act[0].as<bf16>());
+  MSFEM_CUDA(cudaGetLastError());
+  if ((rc = launch_conv<16, 32, cn::EPI_RELU_BF16>(st, B, s->act[0].as<bf16>(), s->wf[0].as<bf16>(),
+                                                  s->bpad[0].as<float>(), nullptr, s->act[1].ptr, 32))) return rc;
+  for (int l = 1; l < 5; ++l)
+    if ((rc = launch_conv<32, 32, cn::EPI_RELU_BF16>(st, B, s->act[l].as<bf16>(), s->wf[l].as<bf16>(),
+                                                    s->bpad[l].as<float>(), nullptr, s->act[l + 1].ptr, 32)))
+      return rc;
+  return launch_conv<32, 16, cn::EPI_F32_NCHW>(st, B, s->act[5].as<bf16>(), s->wf[5].as<bf16>(),
+                                              s->bpad[5].as<float>(), nullptr, out, 4);
+}
+
+// Loss and gradients of one batch into s->grads (FP32) and s->loss (double).
+int surrogate_backward(msfem_surrogate *s, const float *features, const float *targets, int B) {
+  cudaStream_t st = s->h->stream;
+  int rc;
+  if ((rc = surrogate_forward(s, features, B, s->act[cn::kLayers].as<float>()))) return rc;
+  MSFEM_CUDA(cudaMemsetAsync(s->grads.ptr, 0, sizeof(float) * cn::kParams, st));
+  MSFEM_CUDA(cudaMemsetAsync(s->loss.ptr, 0, sizeof(double), st));
+  const float scale = 1.0f / (float)((double)B * 4 * (cn::kH - 2) * (cn::kW - 2));
+  cn::mse_loss_kernel<<<std::max(1, std::min(B * 4, 4096)), 256, 0, st>>>(
+      s->act[cn::kLayers].as<float>(), targets, B, scale, s->ga.as<bf16>(), s->loss.as<double>());
+  MSFEM_CUDA(cudaGetLastError());
+  float *G = s->grads.as<float>();
+  const int sms = s->h->sm_count;
+  auto dW = [&](int l) { return G + cn::param_offset(l); };
+  auto db = [&](int l) { return G + cn::param_offset(l) + (long)cn::real_ch(l + 1) * cn::real_ch(l) * 9; };
+  // layer 6: g (16 ch) in ga
+  if ((rc = launch_wgrad<32, 16>(st, sms, B, s->act[5].as<bf16>(), s->ga.as<bf16>(), 32, 4, dW(5), db(5)))) return rc;
+  if ((rc = launch_conv<16, 32, cn::EPI_MASK_BF16>(st, B, s->ga.as<bf16>(), s->wt[5].as<bf16>(), nullptr,
+                                                  s->act[5].as<bf16>(), s->gb.ptr, 32))) return rc;
+  bf16 *g = s->gb.as<bf16>(), *gn = s->ga.as<bf16>();
+  for (int l = 4; l >= 1; --l) {
+    if ((rc = launch_wgrad<32, 32>(st, sms, B, s->act[l].as<bf16>(), g, 32, 32, dW(l), db(l)))) return rc;
+    if ((rc = launch_conv<32, 32, cn::EPI_MASK_BF16>(st, B, g, s->wt[l].as<bf16>(), nullptr, s->act[l].as<bf16>(),
+                                                    gn, 32))) return rc;
+    std::swap(g, gn);
+  }
+  return launch_wgrad<16, 32>(st, sms, B, s->act[0].as<bf16>(), g, 3, 32, dW(0), db(0));
+}
+
+// The warm start inside msfem_run_batch: features -> prediction -> Q1 + delta.
+int surrogate_warm_start(msfem_handle *h, msfem::KernelParams &p, int nc, int *launches) {
+  msfem_surrogate *s = h->surrogate;
+  const int n = 33 * 33;
+  MSFEM_CUDA(h->feat.ensure(sizeof(float) * (size_t)nc * 3 * n));
+  MSFEM_CUDA(h->delta.ensure(sizeof(float) * (size_t)nc * 4 * n));
+  MSFEM_CUDA(h->warm_pred.ensure(sizeof(double) * (size_t)nc * 4 * n));
+  msfem::features_kernel<<<nc, 256, 0, h->stream>>>(p.qp_values, p.ncomp, p.qp_offset, nc, h->feat.as<float>());
+  MSFEM_CUDA(cudaGetLastError());
+  const int chunk = 4096;
+  int rc;
+  for (int c0 = 0; c0 < nc; c0 += chunk) {
+    const int b = std::min(chunk, nc - c0);
+    if ((rc = surrogate_forward(s, h->feat.as<float>() + (size_t)c0 * 3 * n, b,
+                                h->delta.as<float>() + (size_t)c0 * 4 * n))) return rc;
+    *launches += 7;
+  }
+  msfem::compose_warm_kernel<<<std::min(nc * 4, 8192), 256, 0, h->stream>>>(h->delta.as<float>(), nc,
+                                                                             h->warm_pred.as<double>());
+  MSFEM_CUDA(cudaGetLastError());
+  *launches += 2;
+  p.warm_basis = h->warm_pred.as<double>();
+  return MSFEM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int64_t msfem_surrogate_param_count(void) { return cn::kParams; }
+
+int msfem_surrogate_create(msfem_handle *h, uint64_t seed, msfem_surrogate **out) {
+  if (!h || !out) return fail(MSFEM_ERR_INVALID_ARG, "handle and output are required");
+  MSFEM_CUDA(cudaSetDevice(h->device));
+  auto *s = new msfem_surrogate();
+  s->h = h;
+  // He-uniform weights (last layer scaled down so the first predictions are
+  // near zero), zero biases; SplitMix64 stream
+  std::vector<float> w(cn::kParams, 0.0f);
+  uint64_t state = seed;
+  auto next = [&]() {
+    state += 0x9E3779B97F4A7C15ull;
+    uint64_t z = state;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+  };
+  for (int l = 0; l < cn::kLayers; ++l) {
+    const int cin = cn::real_ch(l), cout = cn::real_ch(l + 1);
+    const double bound = std::sqrt(6.0 / (cin * 9.0)) * (l == cn::kLayers - 1 ? 0.1 : 1.0);
+    float *W = w.data() + cn::param_offset(l);
+    for (long i = 0; i < (long)cout * cin * 9; ++i) W[i] = (float)((2.0 * next() - 1.0) * bound);
+  }
+  int rc = MSFEM_OK;
+  if (s->params.ensure(sizeof(float) * cn::kParams) != cudaSuccess || s->grads.ensure(sizeof(float) * cn::kParams) != cudaSuccess ||
+      s->m.ensure(sizeof(float) * cn::kParams) != cudaSuccess || s->v.ensure(sizeof(float) * cn::kParams) != cudaSuccess ||
+      s->loss.ensure(sizeof(double)) != cudaSuccess)
+    rc = fail(MSFEM_ERR_OUT_OF_MEMORY, "surrogate allocation failed");
+  if (!rc && cudaMemcpyAsync(s->params.ptr, w.data(), sizeof(float) * cn::kParams, cudaMemcpyHostToDevice, h->stream) != cudaSuccess)
+    rc = fail(MSFEM_ERR_CUDA, "surrogate parameter upload failed");
+  if (!rc && (cudaMemsetAsync(s->m.ptr, 0, sizeof(float) * cn::kParams, h->stream) != cudaSuccess ||
+              cudaMemsetAsync(s->v.ptr, 0, sizeof(float) * cn::kParams, h->stream) != cudaSuccess))
+    rc = fail(MSFEM_ERR_CUDA, "surrogate state init failed");
+  if (!rc) rc = surrogate_pack(s);
+  if (!rc && cudaStreamSynchronize(h->stream) != cudaSuccess) rc = fail(MSFEM_ERR_CUDA, "surrogate init failed");
+  if (rc) {
+    msfem_surrogate_destroy(s);
+    return rc;
+  }
+  *out = s;
+  return MSFEM_OK;
+}
+
+int msfem_surrogate_destroy(msfem_surrogate *s) {
+  if (!s) return MSFEM_OK;
+  cudaSetDevice(s->h->device);
+  cudaStreamSynchronize(s->h->stream);
+  if (s->h->surrogate == s) s->h->surrogate = nullptr;
+  DevBuf *bufs[] = {&s->params, &s->grads, &s->m, &s->v, &s->loss, &s->ga, &s->gb};
+  for (DevBuf *b : bufs) b->release();
+  for (int l = 0; l < cn::kLayers; ++l) {
+    s->wf[l].release();
+    s->wt[l].release();
+    s->bpad[l].release();
+  }
+  for (auto &a : s->act) a.release();
+  delete s;
+  return MSFEM_OK;
+}
+
+int msfem_surrogate_set_params(msfem_surrogate *s, const float *params) {
+  if (!s || !params) return fail(MSFEM_ERR_INVALID_ARG, "surrogate and params are required");
+  MSFEM_CUDA(cudaSetDevice(s->h->device));
+  MSFEM_CUDA(cudaMemcpyAsync(s->params.ptr, params, sizeof(float) * cn::kParams, cudaMemcpyHostToDevice, s->h->stream));
+  int rc = surrogate_pack(s);
+  if (rc) return rc;
+  MSFEM_CUDA(cudaStreamSynchronize(s->h->stream));
+  return MSFEM_OK;
+}
+
+int msfem_surrogate_get_params(msfem_surrogate *s, float *params) {
+  if (!s || !params) return fail(MSFEM_ERR_INVALID_ARG, "surrogate and params are required");
+  MSFEM_CUDA(cudaSetDevice(s->h->device));
+  MSFEM_CUDA(cudaMemcpyAsync(params, s->params.ptr, sizeof(float) * cn::kParams, cudaMemcpyDeviceToHost, s->h->stream));
+  MSFEM_CUDA(cudaStreamSynchronize(s->h->stream));
+  return MSFEM_OK;
+}
+
+int msfem_surrogate_features(msfem_handle *h, const msfem_batch_desc *d, float *features) {
+  if (!h) return fail(MSFEM_ERR_INVALID_ARG, "handle is NULL");
+  int rc = validate(d);
+  if (rc) return rc;
+  if (d->dim != 2 || d->n_fine != 32 || d->n_fine_per_cell || d->coef.kind != MSFEM_COEF_TABULATED ||
+      d->memory != MSFEM_MEM_DEVICE)
+    return fail(MSFEM_ERR_UNSUPPORTED, "surrogate features: 2D, N = 32, TABULATED coefficient in device memory");
+  if (d->n_cells == 0) return MSFEM_OK;
+  MSFEM_CUDA(cudaSetDevice(h->device));
+  msfem::features_kernel<<<d->n_cells, 256, 0, h->stream>>>(d->coef.qp_values, d->coef.ncomp, d->coef.qp_offset,
+                                                             d->n_cells, features);
+  MSFEM_CUDA(cudaGetLastError());
+  MSFEM_CUDA(cudaStreamSynchronize(h->stream));
+  return MSFEM_OK;
+}
+
+int msfem_surrogate_targets(msfem_handle *h, const double *basis, int32_t n, float *delta) {
+  if (!h || n < 0 || (n > 0 && (!basis || !delta))) return fail(MSFEM_ERR_INVALID_ARG, "bad surrogate_targets arguments");
+  if (n == 0) return MSFEM_OK;
+  MSFEM_CUDA(cudaSetDevice(h->device));
+  msfem::targets_kernel<<<std::min(n * 4, 8192), 256, 0, h->stream>>>(basis, n, delta);
+  MSFEM_CUDA(cudaGetLastError());
+  MSFEM_CUDA(cudaStreamSynchronize(h->stream));
+  return MSFEM_OK;
+}
+
+int msfem_surrogate_predict(msfem_surrogate *s, const float *features, int32_t n, float *delta) {
+  if (!s || (n > 0 && (!features || !delta))) return fail(MSFEM_ERR_INVALID_ARG, "bad surrogate_predict arguments");
+  MSFEM_CUDA(cudaSetDevice(s->h->device));
+  const int chunk = 4096;
+  for (int c0 = 0; c0 < n; c0 += chunk) {
+    const int b = std::min(chunk, n - c0);
+    int rc = surrogate_forward(s, features + (size_t)c0 * 3 * cn::kPix, b, delta + (size_t)c0 * 4 * cn::kPix);
+    if (rc) return rc;
+  }
+  MSFEM_CUDA(cudaStreamSynchronize(s->h->stream));
+  return MSFEM_OK;
+}
+
+int msfem_surrogate_gradients(msfem_surrogate *s, const float *features, const float *targets, int32_t batch,
+                              float *grads_host, double *loss) {
+  if (!s || batch < 1 || !features || !targets) return fail(MSFEM_ERR_INVALID_ARG, "bad surrogate_gradients arguments");
+  MSFEM_CUDA(cudaSetDevice(s->h->device));
+  int rc = surrogate_backward(s, features, targets, batch);
+  if (rc) return rc;
+  if (grads_host)
+    MSFEM_CUDA(cudaMemcpyAsync(grads_host, s->grads.ptr, sizeof(float) * cn::kParams, cudaMemcpyDeviceToHost, s->h->stream));
+  double l = 0.0;
+  MSFEM_CUDA(cudaMemcpyAsync(&l, s->loss.ptr, sizeof(double), cudaMemcpyDeviceToHost, s->h->stream));
+  MSFEM_CUDA(cudaStreamSynchronize(s->h->stream));
+  if (loss) *loss = l;
+  return MSFEM_OK;
+}
+
+int msfem_surrogate_train_step(msfem_surrogate *s, const float *features, const float *targets, int32_t batch,
+                               float lr, double *loss) {
+  if (!s || batch < 1 || !features || !targets || !(lr > 0.0f))
+    return fail(MSFEM_ERR_INVALID_ARG, "bad surrogate_train_step arguments");
+  MSFEM_CUDA(cudaSetDevice(s->h->device));
+  int rc = surrogate_backward(s, features, targets, batch);
+  if (rc) return rc;
+  s->step++;
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float bc1 = 1.0f - std::pow(b1, (float)s->step), bc2 = 1.0f - std::pow(b2, (float)s->step);
+  cn::adam_kernel<<<64, 256, 0, s->h->stream>>>(s->params.as<float>(), s->grads.as<float>(), s->m.as<float>(),
+                                                s->v.as<float>(), cn::kParams, lr, b1, b2, 1e-8f, bc1, bc2);
+  MSFEM_CUDA(cudaGetLastError());
+  if ((rc = surrogate_pack(s))) return rc;
+  if (loss) {
+    MSFEM_CUDA(cudaMemcpyAsync(loss, s->loss.ptr, sizeof(double), cudaMemcpyDeviceToHost, s->h->stream));
+    MSFEM_CUDA(cudaStreamSynchronize(s->h->stream));
+  }
+  return MSFEM_OK;
+}
+
+int msfem_attach_surrogate(msfem_handle *h, msfem_surrogate *s) {
+  if (!h) return fail(MSFEM_ERR_INVALID_ARG, "handle is NULL");
+  if (s && s->h != h) return fail(MSFEM_ERR_INVALID_ARG, "surrogate belongs to another handle");
+  h->surrogate = s;
+  return MSFEM_OK;
+}
+
+}  // extern "C"
+
 namespace {
 
 // msfem_run_batch with an optional forced launch choice (autotuning).
@@ -847,9 +1222,10 @@ int run_batch_impl(msfem_handle *h, const msfem_batch_desc *d, double *M, double
       if ((rc = upload<int64_t>(h, h->qpoff, off.data(), off.size(), false, &od, &h2d))) return rc;
       p.qp_offset = od;
     }
-  } else if (d->coef.kind == MSFEM_COEF_FOURIER || d->coef.kind == MSFEM_COEF_SPHERES) {
+  } else if (d->coef.kind == MSFEM_COEF_FOURIER || d->coef.kind == MSFEM_COEF_SPHERES ||
+             d->warm_start == MSFEM_WARM_SURROGATE) {
     // tabulate on the device first, then run the tabulated path
-    const int ncomp = (d->coef.kind == MSFEM_COEF_FOURIER && dim == 2) ? 3 : 1;
+    const int ncomp = (d->coef.kind == MSFEM_COEF_SPHERES || dim == 3) ? 1 : 3;
     std::vector<int64_t> off;
     int64_t total = (int64_t)nc * ncomp * nv * ipow(d->n_fine, dim);
     const int64_t *od = nullptr;
@@ -873,6 +1249,12 @@ int run_batch_impl(msfem_handle *h, const msfem_batch_desc *d, double *M, double
     const double *wb = nullptr;
     if ((rc = upload<double>(h, h->warm, d->warm_basis, (size_t)basis_total, dev, &wb, &h2d))) return rc;
     p.warm_basis = wb;
+  }
+  if (d->warm_start == MSFEM_WARM_SURROGATE && nc > 0) {
+    if (!h->surrogate) return fail(MSFEM_ERR_INVALID_ARG, "MSFEM_WARM_SURROGATE: no surrogate attached");
+    if (dim != 2 || d->n_fine_per_cell || d->n_fine != 32)
+      return fail(MSFEM_ERR_UNSUPPORTED, "surrogate warm start: 2D cells with N = 32 only");
+    if ((rc = surrogate_warm_start(h, p, nc, &launches))) return rc;
   }
   p.basis_offset = boffd;
 

@@ -1,0 +1,88 @@
+"""The learned warm start: the GPU forward/backward kernels against the numpy
+FP64 oracle (which itself is checked against finite differences), training,
+and the warm-started solve keeping parity with the cold one."""
+import numpy as np
+import pytest
+
+
+def test_oracle_backward_matches_finite_differences(oracle):
+    from oracle import cnn_oracle as co
+
+    rng = np.random.default_rng(0)
+    n = co.param_count()
+    params = rng.normal(0, 0.3, n) / 3
+    feats = rng.normal(0, 1, (2, 3, 33, 33))
+    tgts = rng.normal(0, 0.1, (2, 4, 33, 33))
+    loss, g = co.loss_and_grads(params, feats, tgts, bf16_mode=False)
+    idx = rng.choice(n, 12, replace=False)
+    for i in idx:
+        e = np.zeros(n)
+        e[i] = 1e-5
+        lp, _ = co.loss_and_grads(params + e, feats, tgts, bf16_mode=False)
+        lm, _ = co.loss_and_grads(params - e, feats, tgts, bf16_mode=False)
+        fd = (lp - lm) / 2e-5
+        assert abs(fd - g[i]) <= 1e-6 + 1e-4 * abs(fd), (i, fd, g[i])
+
+
+def test_param_count_matches_library(built):
+    from oracle import cnn_oracle as co
+
+    lib = built._abi.load()
+    assert lib.msfem_surrogate_param_count() == co.param_count()
+
+
+@pytest.mark.gpu
+def test_gpu_forward_and_gradients_match_oracle(pkg, engine):
+    torch = pytest.importorskip("torch")
+    from oracle import cnn_oracle as co
+
+    sur = pkg.surrogate.Surrogate(engine, seed=7)
+    rng = np.random.default_rng(1)
+    params = (rng.normal(0, 1, sur.n_params) * 0.1).astype(np.float32)
+    sur.set_params(params)
+    feats = rng.normal(0, 1, (3, 3, 33, 33)).astype(np.float32)
+    tgts = rng.normal(0, 0.05, (3, 4, 33, 33)).astype(np.float32)
+    f_d = torch.from_numpy(feats).cuda()
+    t_d = torch.from_numpy(tgts).cuda()
+    out = torch.empty((3, 4, 33, 33), dtype=torch.float32, device="cuda")
+    sur.predict(f_d, out)
+    ref = co.forward(params.astype(np.float64), feats.astype(np.float64), bf16_mode=True)
+    got = out.cpu().numpy()
+    assert np.abs(got - ref).max() <= 2e-3 * np.abs(ref).max()
+    loss, g = sur.gradients(f_d, t_d)
+    lref, gref = co.loss_and_grads(params.astype(np.float64), feats.astype(np.float64),
+                                   tgts.astype(np.float64), bf16_mode=True)
+    assert abs(loss - lref) <= 1e-3 * lref
+    # per layer, relative to the layer's gradient scale (bf16 gradients between layers)
+    off = 0
+    for ws, bs in co.param_shapes():
+        nw, nb = int(np.prod(ws)), int(np.prod(bs))
+        for a, b in ((off, off + nw), (off + nw, off + nw + nb)):
+            scale = np.abs(gref[a:b]).max()
+            assert np.abs(g[a:b] - gref[a:b]).max() <= 2e-2 * scale + 1e-12, (a, b)
+        off += nw + nb
+    sur.close()
+
+
+@pytest.mark.gpu
+def test_training_reduces_loss_and_warm_start_saves_iterations(pkg, engine):
+    torch = pytest.importorskip("torch")
+    S = pkg.surrogate
+    W = pkg.workloads
+    feats, tgts = S.training_set(engine, torch, seeds=[(11, 12, 13), (21, 22, 23)], K=32)
+    sur = S.Surrogate(engine, seed=3)
+    hist = S.train(sur, feats, tgts, torch, epochs=4, batch=128, lr=1e-3)
+    assert hist[-1] < 0.5 * hist[0]
+    # warm-started solve on unseen cells: same answer, fewer iterations
+    prob = W.config2(K=16, N=32, seeds=(3, 30, 300))
+    desc, keep = S.device_problem(engine, prob, torch)
+    cold = S.solve_device(engine, desc, torch, tol=1e-10)
+    sur.attach()
+    warm = S.solve_device(engine, desc, torch, tol=1e-10, warm=pkg._abi.WARM_SURROGATE)
+    sur.detach()
+    assert warm["stats"]["cells_failed"] == 0
+    assert warm["stats"]["max_rel_residual"] < 1e-10
+    Mc, Mw = cold["M"].cpu().numpy(), warm["M"].cpu().numpy()
+    assert np.abs(Mc - Mw).max() < 1e-9 * np.abs(Mc).max()
+    assert warm["stats"]["iterations_total"] < cold["stats"]["iterations_total"]
+    sur.close()
