@@ -867,6 +867,7 @@ int surrogate_forward(msfem_surrogate *s, const float *features, int B, float *o
   cudaStream_t st = s->h->stream;
   int rc;
   if ((rc = surrogate_reserve(s, B))) return rc;
+  if (!out || !features) return fail(MSFEM_ERR_INVALID_ARG, "surrogate forward: NULL buffer");
   cn::features_to_nhwc_kernel<<<std::max(1, std::min(B * 4, 4096)), 256, 0, st>>>(features, B, s->act[0].as<bf16>());
   MSFEM_CUDA(cudaGetLastError());
   if ((rc = launch_conv<16, 32, cn::EPI_RELU_BF16>(st, B, s->act[0].as<bf16>(), s->wf[0].as<bf16>(),
@@ -883,6 +884,8 @@ int surrogate_forward(msfem_surrogate *s, const float *features, int B, float *o
 int surrogate_backward(msfem_surrogate *s, const float *features, const float *targets, int B) {
   cudaStream_t st = s->h->stream;
   int rc;
+  // reserve first: the prediction buffer must exist before its pointer is taken
+  if ((rc = surrogate_reserve(s, B))) return rc;
   if ((rc = surrogate_forward(s, features, B, s->act[cn::kLayers].as<float>()))) return rc;
   MSFEM_CUDA(cudaMemsetAsync(s->grads.ptr, 0, sizeof(float) * cn::kParams, st));
   MSFEM_CUDA(cudaMemsetAsync(s->loss.ptr, 0, sizeof(double), st));
