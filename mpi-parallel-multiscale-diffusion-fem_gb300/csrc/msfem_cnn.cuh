@@ -7,8 +7,10 @@
 //
 //   input    3 channels per node: log a11, a12 / sqrt(a11 a22), log a22
 //            (the tabulated tensor averaged over the node's fine cells)
-//   layers   3 -> 32 -> 32 -> 32 -> 32 -> 32 -> 4, 'same' zero padding, ReLU
-//            after layers 1-5; output = delta_i = phi_i - Q1_i at every node
+//   layers   3 -> 32 -> 32 -> 32 -> 32 -> 32 -> 4, 3x3 kernels with dilations
+//            1, 2, 4, 8, 2, 1 (receptive field 37 x 37: every node sees the
+//            whole cell), 'same' zero padding, ReLU after layers 1-5;
+//            output = delta_i = phi_i - Q1_i at every node
 //   numerics BF16 weights and activations, FP32 accumulation on the tensor
 //            cores (mma.sync m16n8k16 bf16, FP32 accumulators); FP32 master
 //            weights and Adam; the weight gradient is an FP32 reduction.
@@ -32,6 +34,9 @@ constexpr int kLayers = 6;
 // real and padded channel counts per layer boundary (0 = input)
 __host__ __device__ constexpr int real_ch(int i) { return i == 0 ? 3 : (i == kLayers ? 4 : 32); }
 __host__ __device__ constexpr int pad_ch(int i) { return i == 0 ? 16 : (i == kLayers ? 16 : 32); }
+// dilation of layer l (0-based)
+__host__ __device__ constexpr int dilation(int l) { return l == 1 ? 2 : (l == 2 ? 4 : (l == 3 ? 8 : (l == 4 ? 2 : 1))); }
+constexpr int kMaxDil = 8;
 
 // FP32 parameter vector: for each layer W [Cout][Cin][3][3] then b [Cout] (real sizes).
 __host__ __device__ constexpr long param_offset(int layer) {
@@ -63,10 +68,11 @@ enum { EPI_RELU_BF16 = 0,   // out = bf16(relu(acc + b))          (hidden layers
 template <int CIN, int COUT, int EPI>
 __global__ void __launch_bounds__(256)
 conv3x3_kernel(const __nv_bfloat16 *__restrict__ X, const __nv_bfloat16 *__restrict__ Wt,
-               const float *__restrict__ bias, const __nv_bfloat16 *__restrict__ mask, void *out, int cout_real) {
+               const float *__restrict__ bias, const __nv_bfloat16 *__restrict__ mask, void *out, int cout_real,
+               int dil) {
   constexpr int SP = CIN + 8;           // smem pixel pitch (bf16)
   constexpr int WP = 9 * CIN + 8;       // smem weight row pitch (bf16)
-  constexpr int HP = kH + 2;            // halo tile side
+  const int HP = kH + 2 * dil;          // halo tile side
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __nv_bfloat16 *s_in = reinterpret_cast<__nv_bfloat16 *>(smem_raw);
   __nv_bfloat16 *s_w = s_in + HP * HP * SP;
@@ -78,8 +84,8 @@ conv3x3_kernel(const __nv_bfloat16 *__restrict__ X, const __nv_bfloat16 *__restr
     const int pix = i / CH, c8 = (i % CH) * 8;
     const int hy = pix / HP, hx = pix % HP;
     uint4 v = make_uint4(0, 0, 0, 0);
-    if (hy >= 1 && hy <= kH && hx >= 1 && hx <= kW)
-      v = *reinterpret_cast<const uint4 *>(xb + ((hy - 1) * kW + (hx - 1)) * CIN + c8);
+    if (hy >= dil && hy < kH + dil && hx >= dil && hx < kW + dil)
+      v = *reinterpret_cast<const uint4 *>(xb + ((hy - dil) * kW + (hx - dil)) * CIN + c8);
     *reinterpret_cast<uint4 *>(s_in + pix * SP + c8) = v;
   }
   for (int i = tid; i < COUT * 9 * CH; i += 256) {
@@ -90,61 +96,76 @@ conv3x3_kernel(const __nv_bfloat16 *__restrict__ X, const __nv_bfloat16 *__restr
   const int g = lane >> 2, t = lane & 3;
   constexpr int NT = COUT / 8;
   constexpr int MT = (kPix + 15) / 16;
-  for (int mt = warp; mt < MT; mt += 8) {
-    const int pa = mt * 16 + g, pb = pa + 8;
-    const bool va = pa < kPix, vb = pb < kPix;
-    const int ya = va ? pa / kW : 0, xa = va ? pa % kW : 0;
-    const int yb = vb ? pb / kW : 0, xb2 = vb ? pb % kW : 0;
-    float acc[NT][4];
+  constexpr int MB = 3;  // m-tiles per warp pass: each weight fragment feeds MB x NT mma
+  // ldmatrix.x4 row of this lane: pixel (lane & 15) of the m-tile, channel
+  // offset (lane >> 4) * 8; pixels past the image read the (always zero) halo corner
+  const uint32_t s_in_addr = (uint32_t)__cvta_generic_to_shared(s_in);
+  for (int mt0 = warp * MB; mt0 < MT; mt0 += 8 * MB) {
+    float acc[MB][NT][4];
+    int rowbase[MB];
 #pragma unroll
-    for (int n = 0; n < NT; ++n)
+    for (int mb = 0; mb < MB; ++mb) {
 #pragma unroll
-      for (int e = 0; e < 4; ++e) acc[n][e] = 0.f;
+      for (int n = 0; n < NT; ++n)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) acc[mb][n][e] = 0.f;
+      const int pr = (mt0 + mb) * 16 + (lane & 15);
+      rowbase[mb] = pr < kPix ? (pr / kW) * HP + (pr % kW) : -1;
+    }
 #pragma unroll 1
     for (int tap = 0; tap < 9; ++tap) {
-      const int ty = tap / 3, tx = tap % 3;
-      const __nv_bfloat16 *ra = s_in + ((ya + ty) * HP + xa + tx) * SP;
-      const __nv_bfloat16 *rb = s_in + ((yb + ty) * HP + xb2 + tx) * SP;
+      const int toff = (tap / 3) * dil * HP + (tap % 3) * dil;
 #pragma unroll
       for (int ks = 0; ks < CIN / 16; ++ks) {
         const int c0 = ks * 16 + 2 * t;
-        uint32_t a[4];
-        a[0] = va ? ld32(ra + c0) : 0u;
-        a[1] = vb ? ld32(rb + c0) : 0u;
-        a[2] = va ? ld32(ra + c0 + 8) : 0u;
-        a[3] = vb ? ld32(rb + c0 + 8) : 0u;
+        uint32_t bfr[NT][2];
 #pragma unroll
         for (int n = 0; n < NT; ++n) {
           const __nv_bfloat16 *wr = s_w + (n * 8 + g) * WP + tap * CIN + c0;
-          uint32_t bb[2] = {ld32(wr), ld32(wr + 8)};
-          mma_bf16(acc[n], a, bb);
+          bfr[n][0] = ld32(wr);
+          bfr[n][1] = ld32(wr + 8);
+        }
+#pragma unroll
+        for (int mb = 0; mb < MB; ++mb) {
+          const int pix = rowbase[mb] >= 0 ? rowbase[mb] + toff : 0;
+          const uint32_t addr = s_in_addr + (uint32_t)((pix * SP + ks * 16 + (lane >> 4) * 8) * 2);
+          uint32_t a[4];
+          asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                       : "=r"(a[0]), "=r"(a[1]), "=r"(a[2]), "=r"(a[3])
+                       : "r"(addr));
+#pragma unroll
+          for (int n = 0; n < NT; ++n) mma_bf16(acc[mb][n], a, bfr[n]);
         }
       }
     }
-    // epilogue: rows pa / pb, columns n*8 + 2t, +1
+    // epilogue: rows pa / pb of each m-tile, columns n*8 + 2t, +1
 #pragma unroll
-    for (int n = 0; n < NT; ++n) {
-      const int co = n * 8 + 2 * t;
+    for (int mb = 0; mb < MB; ++mb) {
+      const int pa = (mt0 + mb) * 16 + g, pb = pa + 8;
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int p = h ? pb : pa;
-        if (!(h ? vb : va)) continue;
-        float v0 = acc[n][2 * h], v1 = acc[n][2 * h + 1];
-        if (EPI == EPI_RELU_BF16) {
-          v0 = fmaxf(v0 + bias[co], 0.f);
-          v1 = fmaxf(v1 + bias[co + 1], 0.f);
-          __nv_bfloat16 *o = reinterpret_cast<__nv_bfloat16 *>(out) + ((long)b * kPix + p) * COUT + co;
-          *reinterpret_cast<__nv_bfloat162 *>(o) = __floats2bfloat162_rn(v0, v1);
-        } else if (EPI == EPI_F32_NCHW) {
-          float *o = reinterpret_cast<float *>(out) + (long)b * cout_real * kPix + p;
-          if (co < cout_real) o[(long)co * kPix] = v0 + bias[co];
-          if (co + 1 < cout_real) o[(long)(co + 1) * kPix] = v1 + bias[co + 1];
-        } else {
-          const __nv_bfloat16 *mk = mask + ((long)b * kPix + p) * COUT + co;
-          const float m0 = __bfloat162float(mk[0]) > 0.f ? 1.f : 0.f;
-          const float m1 = __bfloat162float(mk[1]) > 0.f ? 1.f : 0.f;
-          __nv_bfloat16 *o = reinterpret_cast<__nv_bfloat16 *>(out) + ((long)b * kPix + p) * COUT + co;
-          *reinterpret_cast<__nv_bfloat162 *>(o) = __floats2bfloat162_rn(v0 * m0, v1 * m1);
+      for (int n = 0; n < NT; ++n) {
+        const int co = n * 8 + 2 * t;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int p = h ? pb : pa;
+          if (p >= kPix) continue;
+          float v0 = acc[mb][n][2 * h], v1 = acc[mb][n][2 * h + 1];
+          if (EPI == EPI_RELU_BF16) {
+            v0 = fmaxf(v0 + bias[co], 0.f);
+            v1 = fmaxf(v1 + bias[co + 1], 0.f);
+            __nv_bfloat16 *o = reinterpret_cast<__nv_bfloat16 *>(out) + ((long)b * kPix + p) * COUT + co;
+            *reinterpret_cast<__nv_bfloat162 *>(o) = __floats2bfloat162_rn(v0, v1);
+          } else if (EPI == EPI_F32_NCHW) {
+            float *o = reinterpret_cast<float *>(out) + (long)b * cout_real * kPix + p;
+            if (co < cout_real) o[(long)co * kPix] = v0 + bias[co];
+            if (co + 1 < cout_real) o[(long)(co + 1) * kPix] = v1 + bias[co + 1];
+          } else {
+            const __nv_bfloat16 *mk = mask + ((long)b * kPix + p) * COUT + co;
+            const float m0 = __bfloat162float(mk[0]) > 0.f ? 1.f : 0.f;
+            const float m1 = __bfloat162float(mk[1]) > 0.f ? 1.f : 0.f;
+            __nv_bfloat16 *o = reinterpret_cast<__nv_bfloat16 *>(out) + ((long)b * kPix + p) * COUT + co;
+            *reinterpret_cast<__nv_bfloat162 *>(o) = __floats2bfloat162_rn(v0 * m0, v1 * m1);
+          }
         }
       }
     }
@@ -152,8 +173,8 @@ conv3x3_kernel(const __nv_bfloat16 *__restrict__ X, const __nv_bfloat16 *__restr
 }
 
 template <int CIN, int COUT>
-constexpr size_t conv_smem() {
-  return sizeof(__nv_bfloat16) * ((size_t)(kH + 2) * (kW + 2) * (CIN + 8) + (size_t)COUT * (9 * CIN + 8));
+constexpr size_t conv_smem(int dil) {
+  return sizeof(__nv_bfloat16) * ((size_t)(kH + 2 * dil) * (kW + 2 * dil) * (CIN + 8) + (size_t)COUT * (9 * CIN + 8));
 }
 
 // Weight/bias gradient of one layer, FP32 accumulation:
@@ -163,8 +184,8 @@ constexpr size_t conv_smem() {
 template <int XC, int GC>
 __global__ void __launch_bounds__(256)
 conv3x3_wgrad_kernel(const __nv_bfloat16 *__restrict__ X, const __nv_bfloat16 *__restrict__ G, int B,
-                     int cin_real, int cout_real, float *__restrict__ dW, float *__restrict__ db) {
-  constexpr int HP = kH + 2;
+                     int cin_real, int cout_real, float *__restrict__ dW, float *__restrict__ db, int dil) {
+  const int HP = kH + 2 * dil;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __nv_bfloat16 *s_x = reinterpret_cast<__nv_bfloat16 *>(smem_raw);   // [HP*HP][XC]
   __nv_bfloat16 *s_g = s_x + HP * HP * XC;                              // [kPix][GC]
@@ -187,8 +208,8 @@ conv3x3_wgrad_kernel(const __nv_bfloat16 *__restrict__ X, const __nv_bfloat16 *_
       const int pix = i / (XC / 8), c8 = (i % (XC / 8)) * 8;
       const int hy = pix / HP, hx = pix % HP;
       uint4 v = make_uint4(0, 0, 0, 0);
-      if (hy >= 1 && hy <= kH && hx >= 1 && hx <= kW)
-        v = *reinterpret_cast<const uint4 *>(xb + ((hy - 1) * kW + (hx - 1)) * XC + c8);
+      if (hy >= dil && hy < kH + dil && hx >= dil && hx < kW + dil)
+        v = *reinterpret_cast<const uint4 *>(xb + ((hy - dil) * kW + (hx - dil)) * XC + c8);
       *reinterpret_cast<uint4 *>(s_x + pix * XC + c8) = v;
     }
     for (int i = tid; i < kPix * (GC / 8); i += 256)
@@ -203,7 +224,7 @@ conv3x3_wgrad_kernel(const __nv_bfloat16 *__restrict__ X, const __nv_bfloat16 *_
         for (int j = 0; j < 4; ++j) gv[j] = (co0 + j < cout_real) ? __bfloat162float(s_g[p * GC + co0 + j]) : 0.f;
 #pragma unroll
         for (int tp = 0; tp < 9; ++tp) {
-          const float xv = __bfloat162float(s_x[((y + tp / 3) * HP + x + tp % 3) * XC + ci]);
+          const float xv = __bfloat162float(s_x[((y + (tp / 3) * dil) * HP + x + (tp % 3) * dil) * XC + ci]);
 #pragma unroll
           for (int j = 0; j < 4; ++j) acc[j][tp] = fmaf(gv[j], xv, acc[j][tp]);
         }
@@ -226,8 +247,8 @@ conv3x3_wgrad_kernel(const __nv_bfloat16 *__restrict__ X, const __nv_bfloat16 *_
 }
 
 template <int XC, int GC>
-constexpr size_t wgrad_smem() {
-  return sizeof(__nv_bfloat16) * ((size_t)(kH + 2) * (kW + 2) * XC + (size_t)kPix * GC);
+constexpr size_t wgrad_smem(int dil) {
+  return sizeof(__nv_bfloat16) * ((size_t)(kH + 2 * dil) * (kW + 2 * dil) * XC + (size_t)kPix * GC);
 }
 
 // Pack the FP32 parameters of layer l into the BF16 forward layout

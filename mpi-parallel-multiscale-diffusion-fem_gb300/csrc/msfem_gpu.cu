@@ -817,22 +817,24 @@ namespace cn = msfem::cnn;
 
 template <int CIN, int COUT, int EPI>
 int launch_conv(cudaStream_t st, int B, const bf16 *X, const bf16 *W, const float *bias, const bf16 *mask,
-                void *out, int cout_real) {
-  const size_t smem = cn::conv_smem<CIN, COUT>();
+                void *out, int cout_real, int dil) {
+  const size_t smem = cn::conv_smem<CIN, COUT>(dil);
   auto fn = cn::conv3x3_kernel<CIN, COUT, EPI>;
-  MSFEM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  fn<<<B, 256, smem, st>>>(X, W, bias, mask, out, cout_real);
+  MSFEM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)cn::conv_smem<CIN, COUT>(cn::kMaxDil)));
+  fn<<<B, 256, smem, st>>>(X, W, bias, mask, out, cout_real, dil);
   MSFEM_CUDA(cudaGetLastError());
   return MSFEM_OK;
 }
 
 template <int XC, int GC>
 int launch_wgrad(cudaStream_t st, int sms, int B, const bf16 *X, const bf16 *G, int cin_real, int cout_real,
-                 float *dW, float *db) {
-  const size_t smem = cn::wgrad_smem<XC, GC>();
+                 float *dW, float *db, int dil) {
+  const size_t smem = cn::wgrad_smem<XC, GC>(dil);
   auto fn = cn::conv3x3_wgrad_kernel<XC, GC>;
-  MSFEM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  fn<<<std::max(1, std::min(B, sms)), 256, smem, st>>>(X, G, B, cin_real, cout_real, dW, db);
+  MSFEM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)cn::wgrad_smem<XC, GC>(cn::kMaxDil)));
+  fn<<<std::max(1, std::min(B, sms)), 256, smem, st>>>(X, G, B, cin_real, cout_real, dW, db, dil);
   MSFEM_CUDA(cudaGetLastError());
   return MSFEM_OK;
 }
@@ -871,13 +873,15 @@ int surrogate_forward(msfem_surrogate *s, const float *features, int B, float *o
   cn::features_to_nhwc_kernel<<<std::max(1, std::min(B * 4, 4096)), 256, 0, st>>>(features, B, s->act[0].as<bf16>());
   MSFEM_CUDA(cudaGetLastError());
   if ((rc = launch_conv<16, 32, cn::EPI_RELU_BF16>(st, B, s->act[0].as<bf16>(), s->wf[0].as<bf16>(),
-                                                  s->bpad[0].as<float>(), nullptr, s->act[1].ptr, 32))) return rc;
+                                                  s->bpad[0].as<float>(), nullptr, s->act[1].ptr, 32,
+                                                  cn::dilation(0)))) return rc;
   for (int l = 1; l < 5; ++l)
     if ((rc = launch_conv<32, 32, cn::EPI_RELU_BF16>(st, B, s->act[l].as<bf16>(), s->wf[l].as<bf16>(),
-                                                    s->bpad[l].as<float>(), nullptr, s->act[l + 1].ptr, 32)))
+                                                    s->bpad[l].as<float>(), nullptr, s->act[l + 1].ptr, 32,
+                                                    cn::dilation(l))))
       return rc;
   return launch_conv<32, 16, cn::EPI_F32_NCHW>(st, B, s->act[5].as<bf16>(), s->wf[5].as<bf16>(),
-                                              s->bpad[5].as<float>(), nullptr, out, 4);
+                                              s->bpad[5].as<float>(), nullptr, out, 4, cn::dilation(5));
 }
 
 // Loss and gradients of one batch into s->grads (FP32) and s->loss (double).
@@ -898,17 +902,19 @@ int surrogate_backward(msfem_surrogate *s, const float *features, const float *t
   auto dW = [&](int l) { return G + cn::param_offset(l); };
   auto db = [&](int l) { return G + cn::param_offset(l) + (long)cn::real_ch(l + 1) * cn::real_ch(l) * 9; };
   // layer 6: g (16 ch) in ga
-  if ((rc = launch_wgrad<32, 16>(st, sms, B, s->act[5].as<bf16>(), s->ga.as<bf16>(), 32, 4, dW(5), db(5)))) return rc;
+  if ((rc = launch_wgrad<32, 16>(st, sms, B, s->act[5].as<bf16>(), s->ga.as<bf16>(), 32, 4, dW(5), db(5),
+                                 cn::dilation(5)))) return rc;
   if ((rc = launch_conv<16, 32, cn::EPI_MASK_BF16>(st, B, s->ga.as<bf16>(), s->wt[5].as<bf16>(), nullptr,
-                                                  s->act[5].as<bf16>(), s->gb.ptr, 32))) return rc;
+                                                  s->act[5].as<bf16>(), s->gb.ptr, 32, cn::dilation(5)))) return rc;
   bf16 *g = s->gb.as<bf16>(), *gn = s->ga.as<bf16>();
   for (int l = 4; l >= 1; --l) {
-    if ((rc = launch_wgrad<32, 32>(st, sms, B, s->act[l].as<bf16>(), g, 32, 32, dW(l), db(l)))) return rc;
+    if ((rc = launch_wgrad<32, 32>(st, sms, B, s->act[l].as<bf16>(), g, 32, 32, dW(l), db(l), cn::dilation(l))))
+      return rc;
     if ((rc = launch_conv<32, 32, cn::EPI_MASK_BF16>(st, B, g, s->wt[l].as<bf16>(), nullptr, s->act[l].as<bf16>(),
-                                                    gn, 32))) return rc;
+                                                    gn, 32, cn::dilation(l)))) return rc;
     std::swap(g, gn);
   }
-  return launch_wgrad<16, 32>(st, sms, B, s->act[0].as<bf16>(), g, 3, 32, dW(0), db(0));
+  return launch_wgrad<16, 32>(st, sms, B, s->act[0].as<bf16>(), g, 3, 32, dW(0), db(0), cn::dilation(0));
 }
 
 // The warm start inside msfem_run_batch: features -> prediction -> Q1 + delta.

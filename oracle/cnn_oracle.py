@@ -1,8 +1,8 @@
 """CPU (numpy FP64) restatement of the learned warm start's network, used as
 the checker of the GPU forward/backward kernels.  TEST INFRASTRUCTURE ONLY.
 
-Network: 6 conv3x3 layers ('same' zero padding), channels 3 -> 32 -> 32 -> 32
--> 32 -> 32 -> 4, ReLU after layers 1-5; loss = mean over (batch, 4 outputs,
+Network: 6 conv3x3 layers ('same' zero padding, dilations 1, 2, 4, 8, 2, 1),
+channels 3 -> 32 -> 32 -> 32 -> 32 -> 32 -> 4, ReLU after layers 1-5; loss = mean over (batch, 4 outputs,
 31 x 31 interior nodes) of (prediction - target)^2.  Parameters are one flat
 vector: per layer W [Cout][Cin][3][3] then b [Cout].
 
@@ -13,6 +13,7 @@ otherwise, so GPU results agree up to FP32 accumulation order.
 import numpy as np
 
 CH = [3, 32, 32, 32, 32, 32, 4]
+DIL = [1, 2, 4, 8, 2, 1]
 H = W = 33
 
 
@@ -48,29 +49,31 @@ def bf16(x):
     return u.astype(np.uint32).view(np.float32).astype(np.float64)
 
 
-def conv(x, w, b=None):
-    """x [B][Cin][H][W], w [Cout][Cin][3][3] -> [B][Cout][H][W] ('same')."""
-    xp = np.pad(x, ((0, 0), (0, 0), (1, 1), (1, 1)))
+def conv(x, w, b=None, d=1):
+    """x [B][Cin][H][W], w [Cout][Cin][3][3] -> [B][Cout][H][W] ('same', dilation d)."""
+    xp = np.pad(x, ((0, 0), (0, 0), (d, d), (d, d)))
     out = np.zeros((x.shape[0], w.shape[0], x.shape[2], x.shape[3]))
     for ty in range(3):
         for tx in range(3):
-            out += np.einsum("bchw,oc->bohw", xp[:, :, ty:ty + x.shape[2], tx:tx + x.shape[3]], w[:, :, ty, tx])
+            sl = xp[:, :, ty * d:ty * d + x.shape[2], tx * d:tx * d + x.shape[3]]
+            out += np.einsum("bchw,oc->bohw", sl, w[:, :, ty, tx])
     if b is not None:
         out += b[None, :, None, None]
     return out
 
 
-def conv_grads(x, w, g):
-    """Gradients of conv(x, w) wrt w, b and x given the output gradient g."""
-    xp = np.pad(x, ((0, 0), (0, 0), (1, 1), (1, 1)))
+def conv_grads(x, w, g, d=1):
+    """Gradients of conv(x, w, d) wrt w, b and x given the output gradient g."""
+    xp = np.pad(x, ((0, 0), (0, 0), (d, d), (d, d)))
     gw = np.zeros_like(w)
     for ty in range(3):
         for tx in range(3):
-            gw[:, :, ty, tx] = np.einsum("bohw,bchw->oc", g, xp[:, :, ty:ty + x.shape[2], tx:tx + x.shape[3]])
+            sl = xp[:, :, ty * d:ty * d + x.shape[2], tx * d:tx * d + x.shape[3]]
+            gw[:, :, ty, tx] = np.einsum("bohw,bchw->oc", g, sl)
     gb = g.sum(axis=(0, 2, 3))
-    # dx = conv(g, flipped/transposed w)
+    # dx = conv(g, flipped/transposed w) at the same dilation
     wt = np.transpose(w[:, :, ::-1, ::-1], (1, 0, 2, 3))
-    gx = conv(g, wt)
+    gx = conv(g, wt, None, d)
     return gw, gb, gx
 
 
@@ -80,7 +83,7 @@ def forward(params, feats, bf16_mode=True, keep=False):
     h = r(feats)
     acts = [h]
     for l, (w, b) in enumerate(layers):
-        z = conv(h, r(w), np.asarray(b, dtype=np.float64))
+        z = conv(h, r(w), np.asarray(b, dtype=np.float64), DIL[l])
         if l < 5:
             h = r(np.maximum(z, 0.0))
         else:
@@ -103,7 +106,7 @@ def loss_and_grads(params, feats, targets, bf16_mode=True):
     grads = [None] * 6
     for l in range(5, -1, -1):
         w, _ = layers[l]
-        gw, gb, gx = conv_grads(acts[l], r(w), g)
+        gw, gb, gx = conv_grads(acts[l], r(w), g, DIL[l])
         grads[l] = (gw, gb)
         if l > 0:
             g = r(gx * (acts[l] > 0))
