@@ -1051,9 +1051,16 @@ msfem2d_mixed_kernel(const KernelParams p) {
       }
       block_sum4(rho);
       const float rho0[4] = {rho[0], rho[1], rho[2], rho[3]};
+      // Inner target: the fixed relative reduction, but never deeper than the
+      // outer goal needs (with a factor 10 margin): ||r|| <= 0.1 tol ||b||.
+      float itol2r[4];
       bool iact[4];
 #pragma unroll
-      for (int r = 0; r < 4; ++r) iact[r] = act[r] > 0.0f && rho[r] > 0.0f;
+      for (int r = 0; r < 4; ++r) {
+        iact[r] = act[r] > 0.0f && rho[r] > 0.0f;
+        const double goal = cs.nu[r] > 0.0 ? 0.01 * tol2 * cs.bb[r] / cs.nu[r] : 0.0;
+        itol2r[r] = fmaxf(itol2, (float)fmin(goal, 0.25));
+      }
       int iit = 0;
       for (;;) {
         if (!(iact[0] || iact[1] || iact[2] || iact[3]) || iit >= p.inner_maxit) break;
@@ -1145,7 +1152,7 @@ msfem2d_mixed_kernel(const KernelParams p) {
           be[r] = 0.0f;
           if (iact[r]) {
             total_iters[r] += 1;
-            if (!(rp[r] <= itol2 * rho0[r]) && isfinite(rp[r])) {
+            if (!(rp[r] <= itol2r[r] * rho0[r]) && isfinite(rp[r])) {
               be[r] = rp[r] / rho[r];
               rho[r] = rp[r];
             } else {

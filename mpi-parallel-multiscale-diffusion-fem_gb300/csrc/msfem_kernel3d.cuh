@@ -749,12 +749,15 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
           buf ^= 1;
         };
         block_sum8(rho);
-        float rho0[8];
+        float rho0[8], itol2r[8];
         bool iact[8];
 #pragma unroll
         for (int r = 0; r < 8; ++r) {
           rho0[r] = rho[r];
           iact[r] = act[r] > 0.0f && rho[r] > 0.0f;
+          // never deeper than the outer goal needs (factor 10 margin)
+          const double goal = cs.nu[r] > 0.0 ? 0.01 * tol2 * cs.bb[r] / cs.nu[r] : 0.0;
+          itol2r[r] = fmaxf(itol2, (float)fmin(goal, 0.25));
         }
         int iit = 0;
         for (;;) {
@@ -800,7 +803,7 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
             be[r] = 0.0f;
             if (iact[r]) {
               total_iters[r] += 1;
-              if (!(rp[r] <= itol2 * rho0[r]) && isfinite(rp[r])) {
+              if (!(rp[r] <= itol2r[r] * rho0[r]) && isfinite(rp[r])) {
                 be[r] = rp[r] / rho[r];
                 rho[r] = rp[r];
               } else {
