@@ -204,6 +204,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 timing (profiling runs)")
     ap.add_argument("--no-config3", action="store_true", help="skip the 65536-cell config-3 timing")
+    ap.add_argument("--no-surrogate", action="store_true", help="skip training / evaluating the warm start")
     ap.add_argument("--coarse", type=int, default=K_COARSE, help="coarse cells per direction")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -426,6 +427,59 @@ def main():
         }
         line["gpu_launches_config3"] = st3 + 2
         del ws3
+        torch.cuda.empty_cache()
+    # ---- learned warm start (the surrogate): trained here with the library's
+    # own BF16 tensor-core forward/backward kernels, evaluated on the unseen
+    # config-3 field (65536 cells) against the cold start
+    if not args.no_surrogate and world == 1 and args.coarse == K_COARSE:
+        S = pkg.surrogate
+        t0 = time.time()
+        feats, tgts = S.training_set(eng, torch)
+        torch.cuda.synchronize()
+        t_data = time.time() - t0
+        sur = S.Surrogate(eng, seed=1)
+        t0 = time.time()
+        hist = S.train(sur, feats, tgts, torch, epochs=20, batch=256, lr=1e-3)
+        torch.cuda.synchronize()
+        t_train = time.time() - t0
+        del feats, tgts
+        desc5, keep5 = S.device_problem(eng, W.config3(), torch)
+        ev = {}
+        for prec, pname in ((abi.PREC_MIXED, "mixed"), (abi.PREC_FP64, "fp64")):
+            for warm, wname in ((abi.WARM_NONE, "cold"), (abi.WARM_SURROGATE, "surrogate")):
+                if warm == abi.WARM_SURROGATE:
+                    sur.attach()
+                S.solve_device(eng, desc5, torch, precision=prec, warm=warm)  # warm-up
+                torch.cuda.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                r = S.solve_device(eng, desc5, torch, precision=prec, warm=warm)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                sur.detach()
+                st = r["stats"]
+                ms = e0.elapsed_time(e1)
+                ev[f"{pname}_{wname}"] = {
+                    "value": st["solves"] / (ms * 1e-3), "unit": UNIT, "ms": ms,
+                    "mean_iterations": st["iterations_total"] / st["solves"],
+                    "max_rel_residual": st["max_rel_residual"], "cells_failed": st["cells_failed"]}
+        for pname in ("mixed", "fp64"):
+            c, w = ev[f"{pname}_cold"], ev[f"{pname}_surrogate"]
+            w["iterations_saved"] = 1.0 - w["mean_iterations"] / c["mean_iterations"]
+            w["speedup_vs_cold"] = c["ms"] / w["ms"]
+        ev["mixed_surrogate"]["speedup_vs_fp64_cold"] = ev["fp64_cold"]["ms"] / ev["mixed_surrogate"]["ms"]
+        line["surrogate"] = {
+            "network": "6 conv3x3 layers 3-32-32-32-32-32-4, dilations 1/2/4/8/2/1, BF16 weights and "
+                       "activations, FP32 accumulation (mma.sync m16n8k16), Adam lr 1e-3",
+            "training": {"solves": int(4 * 12 * 4096), "epochs": 20, "batch": 256,
+                         "data_seconds": t_data, "train_seconds": t_train,
+                         "loss_first_epoch": hist[0], "loss_last_epoch": hist[-1]},
+            "eval_workload": "config 3 field (seeds 3/30/300, not in the training set), 65536 cells",
+            "results": ev,
+        }
+        sur.close()
+        del keep5
         torch.cuda.empty_cache()
     # ---- CPU baseline (rank 0, N = 1 only)
     if rank == 0 and world == 1 and not args.no_cpu:
