@@ -304,6 +304,44 @@ def main():
         _, st = eng.run_desc(d, *args_, stats=True)
         return max_over_ranks(ms), st, clocks
 
+    def solve_with_basis(ws, precision, tol, warm=abi.WARM_NONE, desc=None):
+        """One untimed solve of a device workload with the basis output."""
+        d = desc if desc is not None else device_desc(ws, precision)
+        d.precision, d.tol, d.warm_start = precision, tol, warm
+        n = d.n_cells
+        out = {"M": torch.empty((n, 4, 4), dtype=torch.float64, device=f"cuda:{local}"),
+               "F": torch.empty((n, 4), dtype=torch.float64, device=f"cuda:{local}"),
+               "basis": torch.empty((n, 4, (N_FINE + 1) ** 2), dtype=torch.float64, device=f"cuda:{local}"),
+               "st": torch.empty(n, dtype=torch.int32, device=f"cuda:{local}"),
+               "it": torch.empty((n, 4), dtype=torch.int32, device=f"cuda:{local}")}
+        _, out["stats"] = eng.run_desc(d, out["M"].data_ptr(), out["F"].data_ptr(), out["basis"].data_ptr(),
+                                       out["st"].data_ptr(), out["it"].data_ptr(), stats=True)
+        d.warm_start = abi.WARM_NONE
+        d.tol = TOL
+        return out
+
+    def basis_errors(ws, got, ref, desc=None):
+        """Energy-norm error of every basis function (msfem_energy_error) and
+        the coarse-matrix error of every cell, got against ref."""
+        d = desc if desc is not None else device_desc(ws, abi.PREC_FP64)
+        n = d.n_cells
+        err = torch.empty((n, 4), dtype=torch.float64, device=f"cuda:{local}")
+        nrm = torch.empty((n, 4), dtype=torch.float64, device=f"cuda:{local}")
+        rc = eng.lib.msfem_energy_error(eng.handle, ctypes.byref(d), got["basis"].data_ptr(),
+                                        ref["basis"].data_ptr(), err.data_ptr(), nrm.data_ptr())
+        if rc != abi.OK:
+            raise abi.MsfemError(rc, abi.last_error(eng.lib))
+        torch.cuda.synchronize()
+        rel = err / nrm
+        scale = ref["M"].abs().amax(dim=(1, 2), keepdim=True)
+        mrel = ((got["M"] - ref["M"]).abs() / scale).amax(dim=(1, 2))
+        frel = ((got["F"] - ref["F"]).abs() / ref["F"].abs().amax(dim=1, keepdim=True)).amax(dim=1)
+        return {"max_rel_energy_error": float(rel.max()), "mean_rel_energy_error": float(rel.mean()),
+                "max_rel_M_error": float(mrel.max()), "mean_rel_M_error": float(mrel.mean()),
+                "max_rel_F_error": float(frel.max()),
+                "max_rel_residual": got["stats"]["max_rel_residual"],
+                "cells_failed": got["stats"]["cells_failed"]}
+
     # ---- workload on the device (weak scaling: every rank owns its own
     # 64x64 block of coarse cells, shifted by the rank along x)
     prob = W.config2(K=args.coarse, N=N_FINE)
@@ -426,7 +464,20 @@ def main():
             "speedup_mixed_vs_fp64": ms3f / ms3m,
         }
         line["gpu_launches_config3"] = st3 + 2
+        # per-basis energy-norm and coarse-matrix errors of every cell against
+        # the FP64 form solved to 1e-12 (untimed)
+        ref3 = solve_with_basis(ws3, abi.PREC_FP64, 1e-12)
+        errs = {}
+        for prec, pname in ((abi.PREC_MIXED, "mixed"), (abi.PREC_FP64, "fp64")):
+            errs[pname] = basis_errors(ws3, solve_with_basis(ws3, prec, TOL), ref3)
+        line["config3"]["errors_vs_fp64_1e-12"] = {
+            "reference": "FP64 form solved to 1e-12 relative residual, same cells and field; "
+                         "energy norm ||phi - phi_ref||_A / ||phi_ref||_A per basis function, "
+                         "coarse entries |M_ij - M_ref,ij| / max_ij |M_ref,ij| per cell",
+            "reference_max_rel_residual": ref3["stats"]["max_rel_residual"], **errs}
         del ws3
+        if args.no_surrogate:
+            del ref3
         torch.cuda.empty_cache()
     # ---- learned warm start (the surrogate): trained here with the library's
     # own BF16 tensor-core forward/backward kernels, evaluated on the unseen
@@ -464,6 +515,14 @@ def main():
                     "value": st["solves"] / (ms * 1e-3), "unit": UNIT, "ms": ms,
                     "mean_iterations": st["iterations_total"] / st["solves"],
                     "max_rel_residual": st["max_rel_residual"], "cells_failed": st["cells_failed"]}
+        if not args.no_config3:
+            sur.attach()
+            for prec, pname in ((abi.PREC_MIXED, "mixed"), (abi.PREC_FP64, "fp64")):
+                got = solve_with_basis(None, prec, TOL, warm=abi.WARM_SURROGATE, desc=desc5)
+                ev[f"{pname}_surrogate"]["errors_vs_fp64_1e-12"] = basis_errors(None, got, ref3, desc=desc5)
+                del got
+            sur.detach()
+            del ref3
         for pname in ("mixed", "fp64"):
             c, w = ev[f"{pname}_cold"], ev[f"{pname}_surrogate"]
             w["iterations_saved"] = 1.0 - w["mean_iterations"] / c["mean_iterations"]

@@ -200,6 +200,21 @@ int msfem_run_batch(msfem_handle *handle, const msfem_batch_desc *desc,
                     int32_t *cell_status, int32_t *iterations,
                     msfem_stats *stats);
 
+/* Energy-norm error of every basis function against a reference basis:
+ *   err      [n_cells][2^d]   ||phi_i - ref_i||_A
+ *   ref_norm [n_cells][2^d]   ||ref_i||_A   (= sqrt(M_ii) for a converged ref)
+ * with A the cell's fine Q1 stiffness matrix over all nodes, the
+ * unconstrained diffusion_matrix of diffusion_problem_basis.tpp:159-242
+ * assembled from desc's cells and coefficient, summed element by element.
+ * basis and basis_ref use msfem_run_batch's basis layout.  All four arrays
+ * follow desc->memory; DEVICE calls are asynchronous on the handle's stream.
+ * A malformed cell gets NaN.  No counterpart in the reference (it reports no
+ * basis errors); it serves the error report of the mixed and warm-started
+ * forms against an FP64 solve at a tighter tolerance. */
+int msfem_energy_error(msfem_handle *handle, const msfem_batch_desc *desc,
+                       const double *basis, const double *basis_ref,
+                       double *err, double *ref_norm);
+
 /* Evaluate the coefficient of desc->coef (any analytic kind) at the Gauss
  * points of every fine cell of the batch, in the TABULATED layout, on the
  * device.  qp_values is a device pointer when desc->memory is DEVICE. */

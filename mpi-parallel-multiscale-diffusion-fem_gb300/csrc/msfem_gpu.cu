@@ -1113,42 +1113,15 @@ int msfem_attach_surrogate(msfem_handle *h, msfem_surrogate *s) {
 namespace {
 
 // msfem_run_batch with an optional forced launch choice (autotuning).
-int run_batch_impl(msfem_handle *h, const msfem_batch_desc *d, double *M, double *F,
-                   double *basis, int32_t *cell_status, int32_t *iterations,
-                   msfem_stats *stats, const Tune *force) {
-  const auto t_start = std::chrono::steady_clock::now();
-  if (!h) return fail(MSFEM_ERR_INVALID_ARG, "handle is NULL");
-  int rc = validate(d);
-  if (rc) return rc;
-  if (d->n_cells > 0 && (!M || !F)) return fail(MSFEM_ERR_INVALID_ARG, "M and F are required");
-  MSFEM_CUDA(cudaSetDevice(h->device));
+// Device inputs of a batch (corners, per-cell N, basis offsets, the
+// size-sorted work queue and the coefficient, tabulated on the device for the
+// FOURIER and SPHERES kinds) into the kernel parameters; basis_total is the
+// length of the basis-output layout.
+int prepare_inputs(msfem_handle *h, const msfem_batch_desc *d, const std::vector<int32_t> &nf,
+                   KernelParams &p, int64_t &basis_total, int64_t &h2d, int &launches) {
   const int dim = d->dim, nv = 1 << dim, nc = d->n_cells;
   const bool dev = d->memory == MSFEM_MEM_DEVICE;
-  const bool mixed = d->precision == MSFEM_PREC_MIXED;
-  std::vector<int32_t> nf;
-  if ((rc = host_nfine(h, d, nf))) return rc;
-  int nmax = d->n_fine;
-  if (d->n_fine_per_cell) {
-    nmax = 1;
-    for (int c = 0; c < nc; ++c) nmax = std::max(nmax, nf[c]);
-  }
-  const std::vector<Launch> cands = candidates(dim, nmax, mixed);
-  if (cands.empty())
-    return fail(MSFEM_ERR_UNSUPPORTED, "no kernel for dim " + std::to_string(dim) + ", N " +
-                                           std::to_string(nmax));
-  Tune tn;
-  if (force) {
-    tn = *force;
-  } else {
-    auto it = h->tuning.find(tune_key(dim, nmax, mixed));
-    if (it != h->tuning.end()) tn = it->second;
-  }
-  if (tn.variant < 0 || tn.variant >= (int)cands.size()) tn.variant = 0;
-  const Launch L = cands[tn.variant];
-  int64_t h2d = 0, d2h = 0;
-  int launches = 0;
-
-  // ---- inputs
+  int rc = 0;
   const double *corners = nullptr;
   const int32_t *nfd = nullptr;
   if ((rc = upload<double>(h, h->corners, d->corners, (size_t)nc * nv * dim, dev, &corners, &h2d))) return rc;
@@ -1158,7 +1131,7 @@ int run_batch_impl(msfem_handle *h, const msfem_batch_desc *d, double *M, double
   std::vector<int64_t> boff;
   const int64_t *boffd = nullptr;
   const int32_t *orderd = nullptr;
-  int64_t basis_total = (int64_t)nc * nv * ipow(d->n_fine + 1, dim);
+  basis_total = (int64_t)nc * nv * ipow(d->n_fine + 1, dim);
   if (d->n_fine_per_cell) {
     boff.resize(nc);
     basis_total = 0;
@@ -1178,7 +1151,7 @@ int run_batch_impl(msfem_handle *h, const msfem_batch_desc *d, double *M, double
     if ((rc = upload<int32_t>(h, h->order, order.data(), order.size(), false, &orderd, &h2d))) return rc;
   }
   // coefficient
-  KernelParams p{};
+  p = KernelParams{};
   p.dim = dim;
   p.n_cells = nc;
   p.n_fine_uniform = d->n_fine;
@@ -1186,12 +1159,6 @@ int run_batch_impl(msfem_handle *h, const msfem_batch_desc *d, double *M, double
   p.n_fine = nfd;
   p.order = orderd;
   p.f_value = d->f_value;
-  p.tol = d->tol;
-  p.maxit = d->maxit;
-  p.check_interval = d->check_interval > 0 ? d->check_interval : tn.check_interval;
-  p.inner_tol = tn.inner_tol;
-  p.inner_maxit = std::max(1, std::min(d->maxit, 1000));
-  p.max_refine = 40;
   p.coef_kind = d->coef.kind;
   p.ncomp = d->coef.ncomp;
   for (int k = 0; k < 8; ++k) p.cparams[k] = d->coef.params[k];
@@ -1254,6 +1221,55 @@ int run_batch_impl(msfem_handle *h, const msfem_batch_desc *d, double *M, double
     p.qp_values = h->qp.as<double>();
     p.qp_offset = od;
   }
+  p.basis_offset = boffd;
+  return MSFEM_OK;
+}
+
+int run_batch_impl(msfem_handle *h, const msfem_batch_desc *d, double *M, double *F,
+                   double *basis, int32_t *cell_status, int32_t *iterations,
+                   msfem_stats *stats, const Tune *force) {
+  const auto t_start = std::chrono::steady_clock::now();
+  if (!h) return fail(MSFEM_ERR_INVALID_ARG, "handle is NULL");
+  int rc = validate(d);
+  if (rc) return rc;
+  if (d->n_cells > 0 && (!M || !F)) return fail(MSFEM_ERR_INVALID_ARG, "M and F are required");
+  MSFEM_CUDA(cudaSetDevice(h->device));
+  const int dim = d->dim, nv = 1 << dim, nc = d->n_cells;
+  const bool dev = d->memory == MSFEM_MEM_DEVICE;
+  const bool mixed = d->precision == MSFEM_PREC_MIXED;
+  std::vector<int32_t> nf;
+  if ((rc = host_nfine(h, d, nf))) return rc;
+  int nmax = d->n_fine;
+  if (d->n_fine_per_cell) {
+    nmax = 1;
+    for (int c = 0; c < nc; ++c) nmax = std::max(nmax, nf[c]);
+  }
+  const std::vector<Launch> cands = candidates(dim, nmax, mixed);
+  if (cands.empty())
+    return fail(MSFEM_ERR_UNSUPPORTED, "no kernel for dim " + std::to_string(dim) + ", N " +
+                                           std::to_string(nmax));
+  Tune tn;
+  if (force) {
+    tn = *force;
+  } else {
+    auto it = h->tuning.find(tune_key(dim, nmax, mixed));
+    if (it != h->tuning.end()) tn = it->second;
+  }
+  if (tn.variant < 0 || tn.variant >= (int)cands.size()) tn.variant = 0;
+  const Launch L = cands[tn.variant];
+  int64_t h2d = 0, d2h = 0;
+  int launches = 0;
+
+  // ---- inputs
+  KernelParams p{};
+  int64_t basis_total = 0;
+  if ((rc = prepare_inputs(h, d, nf, p, basis_total, h2d, launches))) return rc;
+  p.tol = d->tol;
+  p.maxit = d->maxit;
+  p.check_interval = d->check_interval > 0 ? d->check_interval : tn.check_interval;
+  p.inner_tol = tn.inner_tol;
+  p.inner_maxit = std::max(1, std::min(d->maxit, 1000));
+  p.max_refine = 40;
   if (d->warm_start == MSFEM_WARM_USER) {
     const double *wb = nullptr;
     if ((rc = upload<double>(h, h->warm, d->warm_basis, (size_t)basis_total, dev, &wb, &h2d))) return rc;
@@ -1265,7 +1281,6 @@ int run_batch_impl(msfem_handle *h, const msfem_batch_desc *d, double *M, double
       return fail(MSFEM_ERR_UNSUPPORTED, "surrogate warm start: 2D cells with N = 32 only");
     if ((rc = surrogate_warm_start(h, p, nc, &launches))) return rc;
   }
-  p.basis_offset = boffd;
 
   // ---- outputs
   auto out_ptr = [&](DevBuf &buf, void *user, size_t bytes) -> void * {
@@ -1443,6 +1458,50 @@ int msfem_run_batch(msfem_handle *h, const msfem_batch_desc *d, double *M, doubl
                     double *basis, int32_t *cell_status, int32_t *iterations,
                     msfem_stats *stats) {
   return run_batch_impl(h, d, M, F, basis, cell_status, iterations, stats, nullptr);
+}
+
+int msfem_energy_error(msfem_handle *h, const msfem_batch_desc *d, const double *basis,
+                       const double *basis_ref, double *err, double *ref_norm) {
+  if (!h) return fail(MSFEM_ERR_INVALID_ARG, "handle is NULL");
+  int rc = validate(d);
+  if (rc) return rc;
+  if (d->n_cells > 0 && (!basis || !basis_ref || !err || !ref_norm))
+    return fail(MSFEM_ERR_INVALID_ARG, "basis, basis_ref, err and ref_norm are required");
+  if (d->n_cells == 0) return MSFEM_OK;
+  MSFEM_CUDA(cudaSetDevice(h->device));
+  const int nv = 1 << d->dim, nc = d->n_cells;
+  const bool dev = d->memory == MSFEM_MEM_DEVICE;
+  std::vector<int32_t> nf;
+  if ((rc = host_nfine(h, d, nf))) return rc;
+  msfem_batch_desc dd = *d;
+  dd.warm_start = MSFEM_WARM_NONE;  // the network is not involved
+  KernelParams p{};
+  int64_t basis_total = 0, h2d = 0;
+  int launches = 0;
+  if ((rc = prepare_inputs(h, &dd, nf, p, basis_total, h2d, launches))) return rc;
+  const double *a = nullptr, *r = nullptr;
+  if ((rc = upload<double>(h, h->basis, basis, (size_t)basis_total, dev, &a, &h2d))) return rc;
+  if ((rc = upload<double>(h, h->warm, basis_ref, (size_t)basis_total, dev, &r, &h2d))) return rc;
+  double *e = err, *n = ref_norm;
+  if (!dev) {
+    MSFEM_CUDA(h->M.ensure(sizeof(double) * nc * nv));
+    MSFEM_CUDA(h->F.ensure(sizeof(double) * nc * nv));
+    e = h->M.as<double>();
+    n = h->F.as<double>();
+  }
+  constexpr int NT = 256;
+  const int grid = std::max(1, std::min(nc, 4 * h->sm_count));
+  if (d->dim == 2)
+    msfem::msfem2d_energy_kernel<NT><<<grid, NT, 0, h->stream>>>(p, a, r, e, n);
+  else
+    msfem::msfem3d_energy_kernel<NT><<<grid, NT, 0, h->stream>>>(p, a, r, e, n);
+  MSFEM_CUDA(cudaGetLastError());
+  if (!dev) {
+    MSFEM_CUDA(cudaMemcpyAsync(err, e, sizeof(double) * nc * nv, cudaMemcpyDeviceToHost, h->stream));
+    MSFEM_CUDA(cudaMemcpyAsync(ref_norm, n, sizeof(double) * nc * nv, cudaMemcpyDeviceToHost, h->stream));
+    MSFEM_CUDA(cudaStreamSynchronize(h->stream));
+  }
+  return MSFEM_OK;
 }
 
 int msfem_set_tuning(msfem_handle *h, const msfem_tuning *t) {

@@ -163,17 +163,11 @@ __device__ __forceinline__ void boundary_node(int k, int N, int &ix, int &iy) {
 // Shared per-cell phases
 // ---------------------------------------------------------------------------
 
-// Geometry, Q1 data, zeroed arrays.  Returns the cell status.
-template <int NMAX, int NT>
-__device__ int cell_begin(const KernelParams &p, CellShared2D &cs, int cell, int N,
-                          double *c64, double *v64, double *d64, float *v32, int tid) {
-  const int P = N + 3, G = P * P;
+// Geometry and Q1 data of one cell (corners, BasisQ1 coefficients, the
+// affine-cell Jacobian data).  Returns the cell status.
+template <int NMAX>
+__device__ int cell_geometry2d(const KernelParams &p, CellShared2D &cs, int cell, int N, int tid) {
   if (tid < 8) cs.corners[tid] = p.corners[(int64_t)cell * 8 + tid];
-  for (int i = tid; i < 4 * G; i += NT) { c64[i] = 0.0; v64[i] = 0.0; }
-  for (int i = tid; i < G; i += NT) d64[i] = 0.0;
-  if (v32)
-    for (int i = tid; i < 4 * G; i += NT) v32[i] = 0.0f;
-  if (tid < 4) { cs.iters[tid] = 0; cs.active[tid] = 1; cs.nu[tid] = 0.0; }
   __syncthreads();
   if (tid == 0) {
     const double *cr = cs.corners;
@@ -205,6 +199,19 @@ __device__ int cell_begin(const KernelParams &p, CellShared2D &cs, int cell, int
   }
   __syncthreads();
   return cs.status;
+}
+
+// Geometry, Q1 data, zeroed arrays.  Returns the cell status.
+template <int NMAX, int NT>
+__device__ int cell_begin(const KernelParams &p, CellShared2D &cs, int cell, int N,
+                          double *c64, double *v64, double *d64, float *v32, int tid) {
+  const int P = N + 3, G = P * P;
+  for (int i = tid; i < 4 * G; i += NT) { c64[i] = 0.0; v64[i] = 0.0; }
+  for (int i = tid; i < G; i += NT) d64[i] = 0.0;
+  if (v32)
+    for (int i = tid; i < 4 * G; i += NT) v32[i] = 0.0f;
+  if (tid < 4) { cs.iters[tid] = 0; cs.active[tid] = 1; cs.nu[tid] = 0.0; }
+  return cell_geometry2d<NMAX>(p, cs, cell, N, tid);
 }
 
 // Malformed cell: NaN outputs and the status word, then move on.
@@ -1217,6 +1224,78 @@ msfem2d_mixed_kernel(const KernelParams p) {
     write_basis<NT>(p, cell, N, v64, d64, tid);
     __syncthreads();  // v32 is reused for the 32-value partials below
     epilogue_finish<NT, true>(p, cs, cell, acc, reinterpret_cast<double *>(v32), true, total_iters, tid);
+  }
+}
+
+// ===========================================================================
+// Energy norms of basis functions against a reference basis
+// ===========================================================================
+// err[cell][i] = ||phi_i - ref_i||_A and nrm[cell][i] = ||ref_i||_A with A the
+// cell's fine Q1 stiffness over all nodes (the unconstrained diffusion_matrix
+// of diffusion_problem_basis.tpp:159-242), summed element by element:
+// e^T A e = sum_c e_c^T K_c e_c.  For a converged ref, nrm^2 = M_ii.  Bases
+// in the basis-output layout ([cell][4][(N+1)^2], lexicographic nodes).
+template <int NT>
+__global__ void __launch_bounds__(NT)
+msfem2d_energy_kernel(const KernelParams p, const double *__restrict__ basis,
+                      const double *__restrict__ ref, double *__restrict__ err,
+                      double *__restrict__ nrm) {
+  constexpr int NW = NT / 32;
+  __shared__ CellShared2D cs;
+  __shared__ double red[NW * 8];
+  __shared__ int bad;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int cell = blockIdx.x; cell < p.n_cells; cell += gridDim.x) {
+    const int N = p.n_fine ? p.n_fine[cell] : p.n_fine_uniform;
+    if (tid == 0) bad = 0;
+    const int st = cell_geometry2d<MSFEM_MAX_N_2D>(p, cs, cell, N, tid);
+    double acc[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) acc[i] = 0.0;
+    if (st == MSFEM_CELL_CONVERGED) {
+      const int n = N + 1, nn = n * n;
+      const int64_t off = p.basis_offset ? p.basis_offset[cell] : (int64_t)cell * 4 * nn;
+      const double *a = basis + off, *r = ref + off;
+      const double *tab = nullptr;
+      if (p.coef_kind == MSFEM_COEF_TABULATED)
+        tab = p.qp_values + (p.qp_offset ? p.qp_offset[cell] : (int64_t)cell * p.ncomp * 4 * N * N);
+      const bool need_x = p.coef_kind != MSFEM_COEF_TABULATED && p.coef_kind != MSFEM_COEF_CONSTANT;
+      for (int fc = tid; fc < N * N; fc += NT) {
+        const int cx = fc % N, cy = fc / N;
+        double Kd[4], Ko[6];
+        if (!element2d(p, cs, tab, N, cx, cy, need_x, Kd, Ko)) bad = 1;
+        const int k0 = cy * n + cx;
+        const int kk[4] = {k0, k0 + 1, k0 + n, k0 + n + 1};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          double e[4], v[4];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            v[j] = r[(int64_t)i * nn + kk[j]];
+            e[j] = a[(int64_t)i * nn + kk[j]] - v[j];
+          }
+          double qe = Kd[0] * e[0] * e[0] + Kd[1] * e[1] * e[1] + Kd[2] * e[2] * e[2] + Kd[3] * e[3] * e[3];
+          double qv = Kd[0] * v[0] * v[0] + Kd[1] * v[1] * v[1] + Kd[2] * v[2] * v[2] + Kd[3] * v[3] * v[3];
+          qe += 2.0 * (Ko[0] * e[0] * e[1] + Ko[1] * e[0] * e[2] + Ko[2] * e[0] * e[3] +
+                       Ko[3] * e[1] * e[2] + Ko[4] * e[1] * e[3] + Ko[5] * e[2] * e[3]);
+          qv += 2.0 * (Ko[0] * v[0] * v[1] + Ko[1] * v[0] * v[2] + Ko[2] * v[0] * v[3] +
+                       Ko[3] * v[1] * v[2] + Ko[4] * v[1] * v[3] + Ko[5] * v[2] * v[3]);
+          acc[i] += qe;
+          acc[4 + i] += qv;
+        }
+      }
+    }
+    warp_partials<8>(acc, red, warp, lane);
+    __syncthreads();
+    if (warp == 0) {
+      const double s = warp_finish<8>(red, NW, lane);
+      if (lane < 8) {
+        double out = sqrt(fmax(s, 0.0));
+        if (st != MSFEM_CELL_CONVERGED || bad || !isfinite(s)) out = qnan();
+        (lane < 4 ? err : nrm)[(int64_t)cell * 4 + (lane & 3)] = out;
+      }
+    }
+    __syncthreads();
   }
 }
 

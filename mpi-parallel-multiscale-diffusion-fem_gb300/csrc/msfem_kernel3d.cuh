@@ -217,6 +217,82 @@ __device__ __forceinline__ void stencil27(const T *__restrict__ c, const T *__re
 
 __device__ __forceinline__ int grid3(int P, int ix, int iy, int iz) { return ((iz + 1) * P + iy + 1) * P + ix + 1; }
 
+// Geometry and Q1 data of one cell: corners, coupling offsets, BasisQ1
+// coefficients, affine-cell Jacobian data and (scalar coefficients on affine
+// cells) the per-Gauss-point element templates.  Sets cs.status.
+template <int NT>
+__device__ void cell_geometry3d(const KernelParams &p, CellShared3D &cs, int cell, int N, bool scalar,
+                                int tid) {
+  const int P = N + 3;
+  if (tid < 24) cs.corners[tid] = p.corners[(int64_t)cell * 24 + tid];
+  if (tid < 13) {
+    int dx, dy, dz;
+    fwd_offset(tid, dx, dy, dz);
+    cs.offs[tid] = (dz * P + dy) * P + dx;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    const double *cr = cs.corners;
+    int st = MSFEM_CELL_CONVERGED;
+    if (N < 1 || N > kNMax3D) st = MSFEM_CELL_BAD_INPUT;
+    if (st == MSFEM_CELL_CONVERGED && !q1_setup<3>(cr, cs.q1coef, cs.q1shift, &cs.q1iscale))
+      st = MSFEM_CELL_BAD_INPUT;
+    // parallelepiped: v_k = v0 + kx e1 + ky e2 + kz e3 exactly
+    int aff = 1;
+    for (int k = 0; k < 8 && aff; ++k)
+      for (int a = 0; a < 3; ++a) {
+        const double pred = cr[a] + ((k & 1) ? cr[3 + a] - cr[a] : 0.0) + ((k & 2) ? cr[6 + a] - cr[a] : 0.0) +
+                            ((k & 4) ? cr[12 + a] - cr[a] : 0.0);
+        if (pred != cr[3 * k + a]) aff = 0;
+      }
+    cs.affine = aff;
+    cs.refinements = 0;
+    if (aff && st == MSFEM_CELL_CONVERGED) {
+      const double invN = 1.0 / (double)N;
+      double J[9];
+      for (int a = 0; a < 3; ++a) {
+        J[3 * a + 0] = (cr[3 + a] - cr[a]) * invN;
+        J[3 * a + 1] = (cr[6 + a] - cr[a]) * invN;
+        J[3 * a + 2] = (cr[12 + a] - cr[a]) * invN;
+      }
+      const double c00 = J[4] * J[8] - J[5] * J[7], c01 = J[5] * J[6] - J[3] * J[8],
+                   c02 = J[3] * J[7] - J[4] * J[6];
+      const double det = J[0] * c00 + J[1] * c01 + J[2] * c02;
+      if (!(det > 0.0)) st = MSFEM_CELL_BAD_INPUT;
+      const double id = 1.0 / det;
+      cs.jinv[0] = c00 * id; cs.jinv[1] = (J[2] * J[7] - J[1] * J[8]) * id; cs.jinv[2] = (J[1] * J[5] - J[2] * J[4]) * id;
+      cs.jinv[3] = c01 * id; cs.jinv[4] = (J[0] * J[8] - J[2] * J[6]) * id; cs.jinv[5] = (J[2] * J[3] - J[0] * J[5]) * id;
+      cs.jinv[6] = c02 * id; cs.jinv[7] = (J[1] * J[6] - J[0] * J[7]) * id; cs.jinv[8] = (J[0] * J[4] - J[1] * J[3]) * id;
+      for (int e = 0; e < 9; ++e) cs.jfine[e] = J[e];
+      cs.absdet = fabs(det);
+    }
+    cs.status = st;
+  }
+  __syncthreads();
+  // element templates for a scalar coefficient on an affine cell:
+  // tmpl[q](i,j) = w|det| (Ji^T grad_i) . (Ji^T grad_j) at Gauss point q
+  if (cs.status == MSFEM_CELL_CONVERGED && cs.affine && scalar) {
+    for (int e = tid; e < 8 * 36; e += NT) {
+      const int q = e / 36, t = e % 36;
+      int i = 0, rem = t;
+      while (rem >= 8 - i) { rem -= 8 - i; ++i; }
+      const int j = i + rem;
+      double gi[3], gj[3];
+      for (int a = 0; a < 3; ++a) {
+        double si = 0.0, sj = 0.0;
+        for (int c = 0; c < 3; ++c) {
+          si += cs.jinv[3 * c + a] * rgrad(i, q, c);
+          sj += cs.jinv[3 * c + a] * rgrad(j, q, c);
+        }
+        gi[a] = si;
+        gj[a] = sj;
+      }
+      cs.tmpl[q][t] = 0.125 * cs.absdet * (gi[0] * gj[0] + gi[1] * gj[1] + gi[2] * gj[2]);
+    }
+  }
+  __syncthreads();
+}
+
 template <int NT, bool MIXED>
 __global__ void __launch_bounds__(NT)
 msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t slot_bytes) {
@@ -254,77 +330,11 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
     float *qq32 = pp32 + 8 * G;
 
     // ---------------- set-up ------------------------------------------
-    if (tid < 24) cs.corners[tid] = p.corners[(int64_t)cell * 24 + tid];
-    if (tid < 13) {
-      int dx, dy, dz;
-      fwd_offset(tid, dx, dy, dz);
-      cs.offs[tid] = (dz * P + dy) * P + dx;
-    }
     if (tid < 8) { cs.iters[tid] = 0; cs.active[tid] = 1; cs.nu[tid] = 0.0; }
     for (long i = tid; i < 22 * G; i += NT) c64[i] = 0.0;  // couplings, diagonal, phi~
-    __syncthreads();
-    if (tid == 0) {
-      const double *cr = cs.corners;
-      int st = MSFEM_CELL_CONVERGED;
-      if (N < 1 || N > kNMax3D) st = MSFEM_CELL_BAD_INPUT;
-      if (st == MSFEM_CELL_CONVERGED && !q1_setup<3>(cr, cs.q1coef, cs.q1shift, &cs.q1iscale))
-        st = MSFEM_CELL_BAD_INPUT;
-      // parallelepiped: v_k = v0 + kx e1 + ky e2 + kz e3 exactly
-      int aff = 1;
-      for (int k = 0; k < 8 && aff; ++k)
-        for (int a = 0; a < 3; ++a) {
-          const double pred = cr[a] + ((k & 1) ? cr[3 + a] - cr[a] : 0.0) + ((k & 2) ? cr[6 + a] - cr[a] : 0.0) +
-                              ((k & 4) ? cr[12 + a] - cr[a] : 0.0);
-          if (pred != cr[3 * k + a]) aff = 0;
-        }
-      cs.affine = aff;
-      cs.refinements = 0;
-      if (aff && st == MSFEM_CELL_CONVERGED) {
-        const double invN = 1.0 / (double)N;
-        double J[9];
-        for (int a = 0; a < 3; ++a) {
-          J[3 * a + 0] = (cr[3 + a] - cr[a]) * invN;
-          J[3 * a + 1] = (cr[6 + a] - cr[a]) * invN;
-          J[3 * a + 2] = (cr[12 + a] - cr[a]) * invN;
-        }
-        const double c00 = J[4] * J[8] - J[5] * J[7], c01 = J[5] * J[6] - J[3] * J[8],
-                     c02 = J[3] * J[7] - J[4] * J[6];
-        const double det = J[0] * c00 + J[1] * c01 + J[2] * c02;
-        if (!(det > 0.0)) st = MSFEM_CELL_BAD_INPUT;
-        const double id = 1.0 / det;
-        cs.jinv[0] = c00 * id; cs.jinv[1] = (J[2] * J[7] - J[1] * J[8]) * id; cs.jinv[2] = (J[1] * J[5] - J[2] * J[4]) * id;
-        cs.jinv[3] = c01 * id; cs.jinv[4] = (J[0] * J[8] - J[2] * J[6]) * id; cs.jinv[5] = (J[2] * J[3] - J[0] * J[5]) * id;
-        cs.jinv[6] = c02 * id; cs.jinv[7] = (J[1] * J[6] - J[0] * J[7]) * id; cs.jinv[8] = (J[0] * J[4] - J[1] * J[3]) * id;
-        for (int e = 0; e < 9; ++e) cs.jfine[e] = J[e];
-        cs.absdet = fabs(det);
-      }
-      cs.status = st;
-    }
-    __syncthreads();
-    // element templates for a scalar coefficient on an affine cell:
-    // tmpl[q](i,j) = w|det| (Ji^T grad_i) . (Ji^T grad_j) at Gauss point q
     const bool scalar = (p.coef_kind == MSFEM_COEF_TABULATED && p.ncomp == 1) ||
                         p.coef_kind == MSFEM_COEF_SINSIN;
-    if (cs.status == MSFEM_CELL_CONVERGED && cs.affine && scalar) {
-      for (int e = tid; e < 8 * 36; e += NT) {
-        const int q = e / 36, t = e % 36;
-        int i = 0, rem = t;
-        while (rem >= 8 - i) { rem -= 8 - i; ++i; }
-        const int j = i + rem;
-        double gi[3], gj[3];
-        for (int a = 0; a < 3; ++a) {
-          double si = 0.0, sj = 0.0;
-          for (int c = 0; c < 3; ++c) {
-            si += cs.jinv[3 * c + a] * rgrad(i, q, c);
-            sj += cs.jinv[3 * c + a] * rgrad(j, q, c);
-          }
-          gi[a] = si;
-          gj[a] = sj;
-        }
-        cs.tmpl[q][t] = 0.125 * cs.absdet * (gi[0] * gj[0] + gi[1] * gj[1] + gi[2] * gj[2]);
-      }
-    }
-    __syncthreads();
+    cell_geometry3d<NT>(p, cs, cell, N, scalar, tid);
     if (cs.status != MSFEM_CELL_CONVERGED) {
       for (int i = tid; i < 64; i += NT) p.M[(int64_t)cell * 64 + i] = __longlong_as_double(0x7ff8000000000000ll);
       if (tid < 8) {
@@ -945,6 +955,86 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
       }
       __syncthreads();
     }
+  }
+}
+
+// Energy norms against a reference basis (3D): err[cell][i] = ||phi_i - ref_i||_A,
+// nrm[cell][i] = ||ref_i||_A, element by element over the fine hexahedra;
+// bases in the basis-output layout ([cell][8][(N+1)^3], lexicographic nodes).
+template <int NT>
+__global__ void __launch_bounds__(NT)
+msfem3d_energy_kernel(const KernelParams p, const double *__restrict__ basis,
+                      const double *__restrict__ ref, double *__restrict__ err,
+                      double *__restrict__ nrm) {
+  constexpr int NW = NT / 32;
+  __shared__ CellShared3D cs;
+  __shared__ double red[NW * 16];
+  __shared__ int bad;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const bool scalar = (p.coef_kind == MSFEM_COEF_TABULATED && p.ncomp == 1) ||
+                      p.coef_kind == MSFEM_COEF_SINSIN;
+  for (int cell = blockIdx.x; cell < p.n_cells; cell += gridDim.x) {
+    const int N = p.n_fine ? p.n_fine[cell] : p.n_fine_uniform;
+    if (tid == 0) bad = 0;
+    cell_geometry3d<NT>(p, cs, cell, N, scalar, tid);
+    const int st = cs.status;
+    double acc[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) acc[i] = 0.0;
+    if (st == MSFEM_CELL_CONVERGED) {
+      const int n = N + 1, nn = n * n * n, nfc = N * N * N;
+      const int64_t off = p.basis_offset ? p.basis_offset[cell] : (int64_t)cell * 8 * nn;
+      const double *a = basis + off, *r = ref + off;
+      const double *tab = nullptr;
+      if (p.coef_kind == MSFEM_COEF_TABULATED)
+        tab = p.qp_values + (p.qp_offset ? p.qp_offset[cell] : (int64_t)cell * p.ncomp * 8 * nfc);
+      const bool need_x = p.coef_kind != MSFEM_COEF_TABULATED && p.coef_kind != MSFEM_COEF_CONSTANT;
+      for (int fc = tid; fc < nfc; fc += NT) {
+        const int cx = fc % N, cy = (fc / N) % N, cz = fc / (N * N);
+        double K[36];
+        if (!element3d(p, cs, tab, N, cx, cy, cz, scalar, need_x, K)) bad = 1;
+        int kk[8];
+#pragma unroll
+        for (int v = 0; v < 8; ++v)
+          kk[v] = (cx + (v & 1)) + n * ((cy + ((v >> 1) & 1)) + n * (cz + (v >> 2)));
+#pragma unroll 1
+        for (int i = 0; i < 8; ++i) {
+          double e[8], w[8];
+#pragma unroll
+          for (int v = 0; v < 8; ++v) {
+            w[v] = r[(int64_t)i * nn + kk[v]];
+            e[v] = a[(int64_t)i * nn + kk[v]] - w[v];
+          }
+          double qe = 0.0, qw = 0.0;
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            double se = 0.5 * K[tri_index(u, u)] * e[u], sw = 0.5 * K[tri_index(u, u)] * w[u];
+#pragma unroll
+            for (int v = u + 1; v < 8; ++v) {
+              se = fma(K[tri_index(u, v)], e[v], se);
+              sw = fma(K[tri_index(u, v)], w[v], sw);
+            }
+            qe = fma(e[u], se, qe);
+            qw = fma(w[u], sw, qw);
+          }
+          // acc[i] is the register array index; i is not unrolled, so select
+#pragma unroll
+          for (int j = 0; j < 8; ++j)
+            if (j == i) { acc[j] += 2.0 * qe; acc[8 + j] += 2.0 * qw; }
+        }
+      }
+    }
+    warp_partials<16>(acc, red, warp, lane);
+    __syncthreads();
+    if (warp == 0) {
+      const double s = warp_finish<16>(red, NW, lane);
+      if (lane < 16) {
+        double out = sqrt(fmax(s, 0.0));
+        if (st != MSFEM_CELL_CONVERGED || bad || !isfinite(s)) out = __longlong_as_double(0x7ff8000000000000ll);
+        (lane < 8 ? err : nrm)[(int64_t)cell * 8 + (lane & 7)] = out;
+      }
+    }
+    __syncthreads();
   }
 }
 

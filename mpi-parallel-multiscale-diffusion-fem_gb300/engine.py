@@ -137,6 +137,23 @@ class Engine:
             raise _abi.MsfemError(rc, _abi.last_error(self.lib))
         return rc, (st.as_dict() if st is not None else None)
 
+    def energy_error(self, problem, basis, basis_ref):
+        """Per basis function ||phi_i - ref_i||_A and ||ref_i||_A (host arrays
+        in the basis-output layout); returns (err, ref_norm) [n_cells][2^d]."""
+        keep = []
+        d = self.make_desc(problem, keep=keep)
+        nc, nv = d.n_cells, 1 << d.dim
+        a = np.ascontiguousarray(basis, dtype=np.float64)
+        r = np.ascontiguousarray(basis_ref, dtype=np.float64)
+        if a.size != self.basis_size(problem) or r.size != a.size:
+            raise ValueError("basis arrays do not match the problem's basis layout")
+        err = np.zeros((nc, nv))
+        nrm = np.zeros((nc, nv))
+        rc = self.lib.msfem_energy_error(self.handle, ctypes.byref(d), _ptr(a), _ptr(r), _ptr(err), _ptr(nrm))
+        if rc != _abi.OK:
+            raise _abi.MsfemError(rc, _abi.last_error(self.lib))
+        return err, nrm
+
     def autotune(self, problem, precision="fp64", tol=1e-10, maxit=1000, sample_cells=1024):
         """Pick the fastest compiled launch shape / parameters for this
         problem's (dim, N class, precision); kept in the handle."""

@@ -180,6 +180,39 @@ def assemble_cell(problem, cell=0):
     return st, bl
 
 
+def energy_norms(problem, basis, basis_ref):
+    """Per cell and basis function ||phi_i - ref_i||_A and ||ref_i||_A with A
+    the oracle's own assembled fine stiffness over all nodes (the
+    unconstrained diffusion_matrix, diffusion_problem_basis.tpp:159-242);
+    bases in the basis-output layout.  Returns (err, ref_norm) [n][2^d]."""
+    dim = problem["dim"]
+    nv = 1 << dim
+    nc = problem["corners"].shape[0]
+    err = np.zeros((nc, nv))
+    nrm = np.zeros((nc, nv))
+    off = 0
+    for c in range(nc):
+        N = int(problem["n_fine_per_cell"][c]) if "n_fine_per_cell" in problem else int(problem["n_fine"])
+        n = N + 1
+        nn = n ** dim
+        st, _ = assemble_cell(problem, c)
+        shape = (n,) * dim  # [z][y][x] (x fastest)
+        for i in range(nv):
+            a = np.asarray(basis[off + i * nn: off + (i + 1) * nn])
+            r = np.asarray(basis_ref[off + i * nn: off + (i + 1) * nn])
+            for vec, out in ((a - r, err), (r, nrm)):
+                v = vec.reshape(shape)
+                vp = np.pad(v, 1)
+                y = np.zeros(nn)
+                for s_ in range(3 ** dim):
+                    o = [(s_ // 3 ** k) % 3 - 1 for k in range(dim)]  # (ox, oy, oz)
+                    sl = tuple(slice(1 + o[dim - 1 - ax], 1 + o[dim - 1 - ax] + n) for ax in range(dim))
+                    y += st[:, s_] * vp[sl].ravel()
+                out[c, i] = np.sqrt(max(float(vec @ y), 0.0))
+        off += nv * nn
+    return err, nrm
+
+
 def basis_q1(problem, cell, x, raw_monomials=False):
     keep = []
     b = make_batch(problem, keep=keep, raw_monomials=raw_monomials)

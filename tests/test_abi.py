@@ -72,6 +72,8 @@ def test_invalid_descriptors_are_rejected_without_a_gpu(built):
     rc = lib.msfem_run_batch(None, None, None, None, None, None, None, None)
     assert rc == abi.ERR_INVALID_ARG
     assert lib.msfem_tabulated_size(None, 1) == -1
+    rc = lib.msfem_energy_error(None, ctypes.byref(d), None, None, None, None)
+    assert rc == abi.ERR_INVALID_ARG
     corners = np.zeros((3, 4, 2))
     d.dim = 2
     d.n_cells = 3
