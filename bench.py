@@ -202,9 +202,11 @@ def main():
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 timing (profiling runs)")
+    ap.add_argument("--profile", default=None, choices=["fp64_2d", "mixed_2d", "fp64_3d", "mixed_3d", "cnn"],
+                    help="run one small single-kernel case (for ncu captures) and exit")
     ap.add_argument("--no-config3", action="store_true", help="skip the 65536-cell config-3 timing")
     ap.add_argument("--no-surrogate", action="store_true", help="skip training / evaluating the warm start")
+    ap.add_argument("--no-config4", action="store_true", help="skip the 3D uneven-N config-4 timing")
     ap.add_argument("--coarse", type=int, default=K_COARSE, help="coarse cells per direction")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -235,16 +237,12 @@ def main():
             torch.distributed.barrier()
 
     def max_over_ranks(x):
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
+        return pkg.sharding.max_over_ranks(x, torch.distributed if world > 1 else None, f"cuda:{local}")
 
     def make_ws(prob, shift):
         """Device workload: corners + the coefficient tabulated at the Gauss
         points (input data, tabulated once by the library's field kernel)."""
-        corners_h = np.ascontiguousarray(prob["corners"] + np.array([float(shift), 0.0]))
+        corners_h = pkg.sharding.weak_shard_corners(prob["corners"], shift)
         n = corners_h.shape[0]
         corners_d = torch.from_numpy(corners_h).to(f"cuda:{local}")
         modes_d = torch.from_numpy(np.ascontiguousarray(prob["coef"]["modes"])).to(f"cuda:{local}")
@@ -342,6 +340,52 @@ def main():
                 "max_rel_residual": got["stats"]["max_rel_residual"],
                 "cells_failed": got["stats"]["cells_failed"]}
 
+    # ---- small single-kernel cases for ncu captures (--profile KIND): W
+    # warm-up launches, then K timed ones; nothing else runs
+    if args.profile:
+        kind = args.profile
+        t_ms = None
+        if kind in ("fp64_2d", "mixed_2d"):
+            # 48x48 cells: a 226 MB tabulated field, larger than L2
+            wsp = make_ws(W.config2(K=48, N=N_FINE), 0)
+            prec = abi.PREC_FP64 if kind == "fp64_2d" else abi.PREC_MIXED
+            t_ms, _, _ = timed_ws(wsp, prec, args.steps, args.warmup)
+        elif kind in ("fp64_3d", "mixed_3d"):
+            # the first 256 cells of config 4 (uneven N, 1e4-contrast spheres)
+            sub = W.subset(W.config4(), np.arange(256))
+            prec = "fp64" if kind == "fp64_3d" else "mixed"
+            for _ in range(args.warmup):
+                eng.run(sub, precision=prec, tol=TOL)
+            t_ms = 0.0
+            for _ in range(args.steps):
+                t_ms += eng.run(sub, precision=prec, tol=TOL)["stats"]["kernel_ms"] / args.steps
+        elif kind == "cnn":
+            # inference of 2048 cells and training steps of batch 256 (random weights)
+            S = pkg.surrogate
+            desc_p, keep_p = S.device_problem(eng, W.subset(W.config2(K=64, N=N_FINE), np.arange(2048)), torch)
+            feats = S.features(eng, desc_p, torch)
+            sur = S.Surrogate(eng, seed=7)
+            out = torch.empty((2048, 4, 33, 33), dtype=torch.float32, device=f"cuda:{local}")
+            tg = torch.zeros((256, 4, 33, 33), dtype=torch.float32, device=f"cuda:{local}")
+            for _ in range(args.warmup):
+                sur.predict(feats, out)
+                sur.train_step(feats[:256].contiguous(), tg, 1e-3)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(args.steps):
+                sur.predict(feats, out)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            t_ms = e0.elapsed_time(e1) / args.steps
+            for _ in range(args.steps):
+                sur.train_step(feats[:256].contiguous(), tg, 1e-3)
+            torch.cuda.synchronize()
+            sur.close()
+        print(json.dumps({"profile": kind, "ms_per_step": t_ms, "steps": args.steps, "warmup": args.warmup}))
+        return
+
     # ---- workload on the device (weak scaling: every rank owns its own
     # 64x64 block of coarse cells, shifted by the rank along x)
     prob = W.config2(K=args.coarse, N=N_FINE)
@@ -354,12 +398,8 @@ def main():
         return timed_ws(ws2, precision, steps, warmup, sample_clocks)
 
     # ---- FP64 form (headline)
-    if args.no_fp64:
-        msmx, stmx, _ = timed(abi.PREC_MIXED, args.steps, args.warmup)
-        print(json.dumps({"profile_only": "mixed", "ms_per_step": msmx}))
-        return
     ms64, st64, clocks = timed(abi.PREC_FP64, args.steps, args.warmup, sample_clocks=True)
-    value = world * solves_rank / (ms64 * 1e-3)
+    value = pkg.sharding.job_throughput(world * solves_rank, ms64 * 1e-3)
     probe = load_probe(pkg)
     fp64_peak = ctypes.c_double(0.0)
     fp32_peak = ctypes.c_double(0.0)
@@ -478,6 +518,81 @@ def main():
         del ws3
         if args.no_surrogate:
             del ref3
+        torch.cuda.empty_cache()
+    # ---- config 4: 3D unit cube, 16^3 coarse cells with uneven N in {8,16,24},
+    # 1e4-contrast spheres, 8 RHS; one persistent kernel per call, autotuned
+    # on a sample of the batch, FP64 and mixed
+    if not args.no_config4 and world == 1 and args.coarse == K_COARSE:
+        t0 = time.time()
+        prob4 = W.config4()
+        t_rsa = time.time() - t0
+        nc4 = prob4["corners"].shape[0]
+        nf4_h = np.ascontiguousarray(prob4["n_fine_per_cell"], dtype=np.int32)
+        corners4 = torch.from_numpy(np.ascontiguousarray(prob4["corners"])).to(f"cuda:{local}")
+        nf4 = torch.from_numpy(nf4_h).to(f"cuda:{local}")
+        sp4 = np.ascontiguousarray(prob4["coef"]["spheres"])
+        size4 = int(np.sum(8 * nf4_h.astype(np.int64) ** 3))
+        tab4 = torch.empty(size4, dtype=torch.float64, device=f"cuda:{local}")
+        dt = abi.BatchDesc()
+        dt.dim, dt.n_cells, dt.n_fine = 3, nc4, 24
+        dt.corners, dt.n_fine_per_cell = corners4.data_ptr(), nf4.data_ptr()
+        dt.coef.kind = abi.COEF_SPHERES
+        dt.coef.params[0] = float(prob4["coef"]["params"][0])
+        dt.coef.spheres = sp4.ctypes.data
+        dt.coef.n_spheres = sp4.shape[0]
+        dt.memory = abi.MEM_DEVICE
+        dt.f_value, dt.tol, dt.maxit = 1.0, TOL, 1000
+        rc = eng.lib.msfem_tabulate_coefficient(eng.handle, ctypes.byref(dt), 1, tab4.data_ptr())
+        if rc != abi.OK:
+            raise abi.MsfemError(rc, abi.last_error(eng.lib))
+
+        def desc4(precision, n=nc4):
+            d = abi.BatchDesc()
+            d.dim, d.n_cells, d.n_fine = 3, n, 24
+            d.precision = precision
+            d.corners, d.n_fine_per_cell = corners4.data_ptr(), nf4.data_ptr()
+            d.coef.kind, d.coef.ncomp, d.coef.qp_values = abi.COEF_TABULATED, 1, tab4.data_ptr()
+            d.f_value, d.tol, d.maxit, d.memory = 1.0, TOL, 1000, abi.MEM_DEVICE
+            return d
+
+        M4 = torch.empty((nc4, 8, 8), dtype=torch.float64, device=f"cuda:{local}")
+        F4 = torch.empty((nc4, 8), dtype=torch.float64, device=f"cuda:{local}")
+        st4 = torch.empty(nc4, dtype=torch.int32, device=f"cuda:{local}")
+        it4 = torch.empty((nc4, 8), dtype=torch.int32, device=f"cuda:{local}")
+        res4 = {"workload": "3D 16^3 coarse cells, N per cell uniform over {8,16,24} (seed 4), "
+                            "a = 1 + (1e4 - 1) [x in spheres], spheres r in [0.004, 0.012] at volume "
+                            "fraction 0.2 (seed 44, random sequential addition), f=1, 8 RHS, "
+                            "1e-10 rel residual",
+                "cells_by_N": {str(v): int((nf4_h == v).sum()) for v in (8, 16, 24)},
+                "spheres": int(sp4.shape[0]), "sphere_generation_s": t_rsa}
+        for prec, pname in ((abi.PREC_FP64, "fp64"), (abi.PREC_MIXED, "mixed")):
+            # autotune on the first 512 cells (the same N mix), then time the batch
+            tn = abi.Tuning()
+            rc = eng.lib.msfem_autotune(eng.handle, ctypes.byref(desc4(prec, 512)), 512, ctypes.byref(tn))
+            if rc != abi.OK:
+                raise abi.MsfemError(rc, abi.last_error(eng.lib))
+            d = desc4(prec)
+            outs = (M4.data_ptr(), F4.data_ptr(), None, st4.data_ptr(), it4.data_ptr())
+            eng.run_desc(d, *outs, stats=False)  # warm-up
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            eng.run_desc(d, *outs, stats=False)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            _, s4 = eng.run_desc(d, *outs, stats=True)
+            it_h = it4.cpu().numpy()
+            res4[pname] = {"value": 8 * nc4 / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms,
+                           "mean_iterations": s4["iterations_total"] / s4["solves"],
+                           "mean_iterations_by_N": {str(v): float(it_h[nf4_h == v].mean()) for v in (8, 16, 24)},
+                           "max_refinements": s4["refinements_max"],
+                           "max_rel_residual": s4["max_rel_residual"], "cells_failed": s4["cells_failed"],
+                           "tuning": tn.as_dict()}
+        res4["speedup_mixed_vs_fp64"] = res4["fp64"]["ms_per_step"] / res4["mixed"]["ms_per_step"]
+        line["config4"] = res4
+        del tab4, M4, F4, st4, it4, corners4, nf4
         torch.cuda.empty_cache()
     # ---- learned warm start (the surrogate): trained here with the library's
     # own BF16 tensor-core forward/backward kernels, evaluated on the unseen

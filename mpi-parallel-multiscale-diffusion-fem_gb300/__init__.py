@@ -7,5 +7,5 @@ include/msfem_gpu.h; this package builds it (build.py), binds it (_abi.py,
 engine.py) and describes workloads (workloads.py).  It is imported under the
 name ``msfem_gb300`` (the folder name is not an identifier).
 """
-from . import _abi, build, engine, surrogate, workloads  # noqa: F401
+from . import _abi, build, engine, sharding, surrogate, workloads  # noqa: F401
 from .engine import Engine  # noqa: F401
