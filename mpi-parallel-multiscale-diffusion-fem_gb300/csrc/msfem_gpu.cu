@@ -21,6 +21,7 @@
 #include "msfem_kernel2d.cuh"
 #include "msfem_kernel3d.cuh"
 #include "msfem_cnn.cuh"
+#include "msfem_conv_tc.cuh"
 #include "msfem_gpu.h"
 
 namespace {
@@ -807,7 +808,8 @@ struct msfem_surrogate {
   DevBuf params, grads, m, v, loss;
   DevBuf wf[msfem::cnn::kLayers], wt[msfem::cnn::kLayers], bpad[msfem::cnn::kLayers];
   DevBuf act[msfem::cnn::kLayers + 1];  // act[0] input, act[1..5] hidden, act[6] FP32 prediction
-  DevBuf ga, gb;                        // gradient ping-pong (NHWC bf16)
+  DevBuf ga, gb;                        // gradient ping-pong (channel-blocked bf16)
+  DevBuf tc_err;                        // int: timeout code of the tensor-core convolution (0 = none)
 };
 
 namespace {
@@ -815,16 +817,85 @@ namespace {
 using bf16 = __nv_bfloat16;
 namespace cn = msfem::cnn;
 
+// cuTensorMapEncodeTiled from the driver (no link-time dependency on libcuda).
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn tensor_map_encoder() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  return fn;
+}
+
+// One 3x3 convolution layer on the tcgen05 tensor cores: X (channel-blocked
+// bf16) through a TMA tensor map (one box of (33 + 2 dil) pixels x the window
+// rows per 8-channel block), persistent CTAs capped so that their TMEM
+// columns fit the SM's 512.
 template <int CIN, int COUT, int EPI>
-int launch_conv(cudaStream_t st, int B, const bf16 *X, const bf16 *W, const float *bias, const bf16 *mask,
+int launch_conv(msfem_surrogate *s, int B, const bf16 *X, const bf16 *W, const float *bias, const bf16 *mask,
                 void *out, int cout_real, int dil) {
-  const size_t smem = cn::conv_smem<CIN, COUT>(dil);
-  auto fn = cn::conv3x3_kernel<CIN, COUT, EPI>;
+  if (B <= 0) return MSFEM_OK;
+  const EncodeTiledFn enc = tensor_map_encoder();
+  if (!enc) return fail(MSFEM_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+  const cn::tc::ConvGeom g = cn::tc::conv_geom(dil);
+  // blocked layout [B][CIN/8][33][33][8] viewed as 8-byte elements: dims (66
+  // per row = 33 pixels x 2, 33 rows, B * CIN/8 blocks); a box row is a
+  // contiguous run of wp pixels (2 wp elements <= 98, within the 256 limit).
+  // Two maps: boxes of kBoxRows rows and one of the remaining window rows.
+  const cuuint64_t dims[3] = {2u * cn::kW, (cuuint64_t)cn::kH, (cuuint64_t)B * (CIN / 8)};
+  const cuuint64_t strides[2] = {(cuuint64_t)cn::kW * 16, (cuuint64_t)cn::kPix * 16};
+  const cuuint32_t estr[3] = {1u, 1u, 1u};
+  const int rem = g.box_rows % cn::tc::kBoxRows;
+  CUtensorMap maps[2];
+  for (int m = 0; m < 2; ++m) {
+    const cuuint32_t rows = m == 0 ? (cuuint32_t)cn::tc::kBoxRows : (cuuint32_t)std::max(rem, 1);
+    const cuuint32_t box[3] = {2u * (cuuint32_t)g.wp, rows, 1u};
+    const CUresult r = enc(&maps[m], CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, const_cast<bf16 *>(X), dims, strides, box,
+                           estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS)
+      return fail(MSFEM_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+  }
+  auto fn = cn::tc::conv3x3_tc_kernel<CIN, COUT, EPI>;
+  const size_t smem = cn::tc::conv_tc_smem<CIN, COUT>(dil);
   MSFEM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)cn::conv_smem<CIN, COUT>(cn::kMaxDil)));
-  fn<<<B, 256, smem, st>>>(X, W, bias, mask, out, cout_real, dil);
+                                  (int)cn::tc::conv_tc_smem<CIN, COUT>(cn::kMaxDil)));
+  // all of the unified L1/shared storage as shared memory, so that several
+  // CTAs fit from the first launch on
+  MSFEM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                  (int)cudaSharedmemCarveoutMaxShared));
+  // CTAs per SM from the shared-memory capacity and the 512 TMEM columns
+  // (an SM never holds more accumulator sets than fit)
+  int smem_sm = 0, smem_rsv = 0;
+  MSFEM_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, s->h->device));
+  MSFEM_CUDA(cudaDeviceGetAttribute(&smem_rsv, cudaDevAttrReservedSharedMemoryPerBlock, s->h->device));
+  int per_sm = smem_sm / (int)(smem + smem_rsv + 256);  // + static shared memory (<= 208 B)
+  per_sm = std::min(per_sm, 512 / (cn::tc::kStages * cn::tc::kTiles * COUT));
+  if (per_sm < 1) return fail(MSFEM_ERR_UNSUPPORTED, "tensor-core convolution does not fit on an SM");
+  const long items = (long)B * g.segs;
+  const int grid = (int)std::min<long>(items, (long)per_sm * s->h->sm_count);
+  fn<<<grid, cn::tc::kThreads, smem, s->h->stream>>>(maps[0], maps[1], W, bias, mask, out, cout_real, dil, B,
+                                                      s->tc_err.as<int>());
   MSFEM_CUDA(cudaGetLastError());
   return MSFEM_OK;
+}
+
+// After a synchronisation: report (and clear) a timeout of the tensor-core
+// convolution's pipeline.
+int surrogate_check(msfem_surrogate *s) {
+  int code = 0;
+  MSFEM_CUDA(cudaMemcpy(&code, s->tc_err.ptr, sizeof(int), cudaMemcpyDeviceToHost));
+  if (!code) return MSFEM_OK;
+  MSFEM_CUDA(cudaMemset(s->tc_err.ptr, 0, sizeof(int)));
+  return fail(MSFEM_ERR_CUDA, std::string("tensor-core convolution timed out in its ") +
+                                  (code == 1 ? "window loads (TMA)" : code == 2 ? "MMA issue" : "epilogue"));
 }
 
 template <int XC, int GC>
@@ -870,17 +941,17 @@ int surrogate_forward(msfem_surrogate *s, const float *features, int B, float *o
   int rc;
   if ((rc = surrogate_reserve(s, B))) return rc;
   if (!out || !features) return fail(MSFEM_ERR_INVALID_ARG, "surrogate forward: NULL buffer");
-  cn::features_to_nhwc_kernel<<<std::max(1, std::min(B * 4, 4096)), 256, 0, st>>>(features, B, s->act[0].as<bf16>());
+  cn::features_to_blocked_kernel<<<std::max(1, std::min(B * 4, 4096)), 256, 0, st>>>(features, B, s->act[0].as<bf16>());
   MSFEM_CUDA(cudaGetLastError());
-  if ((rc = launch_conv<16, 32, cn::EPI_RELU_BF16>(st, B, s->act[0].as<bf16>(), s->wf[0].as<bf16>(),
+  if ((rc = launch_conv<16, 32, cn::EPI_RELU_BF16>(s, B, s->act[0].as<bf16>(), s->wf[0].as<bf16>(),
                                                   s->bpad[0].as<float>(), nullptr, s->act[1].ptr, 32,
                                                   cn::dilation(0)))) return rc;
   for (int l = 1; l < 5; ++l)
-    if ((rc = launch_conv<32, 32, cn::EPI_RELU_BF16>(st, B, s->act[l].as<bf16>(), s->wf[l].as<bf16>(),
+    if ((rc = launch_conv<32, 32, cn::EPI_RELU_BF16>(s, B, s->act[l].as<bf16>(), s->wf[l].as<bf16>(),
                                                     s->bpad[l].as<float>(), nullptr, s->act[l + 1].ptr, 32,
                                                     cn::dilation(l))))
       return rc;
-  return launch_conv<32, 16, cn::EPI_F32_NCHW>(st, B, s->act[5].as<bf16>(), s->wf[5].as<bf16>(),
+  return launch_conv<32, 16, cn::EPI_F32_NCHW>(s, B, s->act[5].as<bf16>(), s->wf[5].as<bf16>(),
                                               s->bpad[5].as<float>(), nullptr, out, 4, cn::dilation(5));
 }
 
@@ -904,13 +975,13 @@ int surrogate_backward(msfem_surrogate *s, const float *features, const float *t
   // layer 6: g (16 ch) in ga
   if ((rc = launch_wgrad<32, 16>(st, sms, B, s->act[5].as<bf16>(), s->ga.as<bf16>(), 32, 4, dW(5), db(5),
                                  cn::dilation(5)))) return rc;
-  if ((rc = launch_conv<16, 32, cn::EPI_MASK_BF16>(st, B, s->ga.as<bf16>(), s->wt[5].as<bf16>(), nullptr,
+  if ((rc = launch_conv<16, 32, cn::EPI_MASK_BF16>(s, B, s->ga.as<bf16>(), s->wt[5].as<bf16>(), nullptr,
                                                   s->act[5].as<bf16>(), s->gb.ptr, 32, cn::dilation(5)))) return rc;
   bf16 *g = s->gb.as<bf16>(), *gn = s->ga.as<bf16>();
   for (int l = 4; l >= 1; --l) {
     if ((rc = launch_wgrad<32, 32>(st, sms, B, s->act[l].as<bf16>(), g, 32, 32, dW(l), db(l), cn::dilation(l))))
       return rc;
-    if ((rc = launch_conv<32, 32, cn::EPI_MASK_BF16>(st, B, g, s->wt[l].as<bf16>(), nullptr, s->act[l].as<bf16>(),
+    if ((rc = launch_conv<32, 32, cn::EPI_MASK_BF16>(s, B, g, s->wt[l].as<bf16>(), nullptr, s->act[l].as<bf16>(),
                                                     gn, 32, cn::dilation(l)))) return rc;
     std::swap(g, gn);
   }
@@ -974,8 +1045,10 @@ int msfem_surrogate_create(msfem_handle *h, uint64_t seed, msfem_surrogate **out
   int rc = MSFEM_OK;
   if (s->params.ensure(sizeof(float) * cn::kParams) != cudaSuccess || s->grads.ensure(sizeof(float) * cn::kParams) != cudaSuccess ||
       s->m.ensure(sizeof(float) * cn::kParams) != cudaSuccess || s->v.ensure(sizeof(float) * cn::kParams) != cudaSuccess ||
-      s->loss.ensure(sizeof(double)) != cudaSuccess)
+      s->loss.ensure(sizeof(double)) != cudaSuccess || s->tc_err.ensure(sizeof(int)) != cudaSuccess)
     rc = fail(MSFEM_ERR_OUT_OF_MEMORY, "surrogate allocation failed");
+  if (!rc && cudaMemsetAsync(s->tc_err.ptr, 0, sizeof(int), h->stream) != cudaSuccess)
+    rc = fail(MSFEM_ERR_CUDA, "surrogate state init failed");
   if (!rc && cudaMemcpyAsync(s->params.ptr, w.data(), sizeof(float) * cn::kParams, cudaMemcpyHostToDevice, h->stream) != cudaSuccess)
     rc = fail(MSFEM_ERR_CUDA, "surrogate parameter upload failed");
   if (!rc && (cudaMemsetAsync(s->m.ptr, 0, sizeof(float) * cn::kParams, h->stream) != cudaSuccess ||
@@ -996,7 +1069,7 @@ int msfem_surrogate_destroy(msfem_surrogate *s) {
   cudaSetDevice(s->h->device);
   cudaStreamSynchronize(s->h->stream);
   if (s->h->surrogate == s) s->h->surrogate = nullptr;
-  DevBuf *bufs[] = {&s->params, &s->grads, &s->m, &s->v, &s->loss, &s->ga, &s->gb};
+  DevBuf *bufs[] = {&s->params, &s->grads, &s->m, &s->v, &s->loss, &s->ga, &s->gb, &s->tc_err};
   for (DevBuf *b : bufs) b->release();
   for (int l = 0; l < cn::kLayers; ++l) {
     s->wf[l].release();
@@ -1062,7 +1135,7 @@ int msfem_surrogate_predict(msfem_surrogate *s, const float *features, int32_t n
     if (rc) return rc;
   }
   MSFEM_CUDA(cudaStreamSynchronize(s->h->stream));
-  return MSFEM_OK;
+  return surrogate_check(s);
 }
 
 int msfem_surrogate_gradients(msfem_surrogate *s, const float *features, const float *targets, int32_t batch,
@@ -1077,7 +1150,7 @@ int msfem_surrogate_gradients(msfem_surrogate *s, const float *features, const f
   MSFEM_CUDA(cudaMemcpyAsync(&l, s->loss.ptr, sizeof(double), cudaMemcpyDeviceToHost, s->h->stream));
   MSFEM_CUDA(cudaStreamSynchronize(s->h->stream));
   if (loss) *loss = l;
-  return MSFEM_OK;
+  return surrogate_check(s);
 }
 
 int msfem_surrogate_train_step(msfem_surrogate *s, const float *features, const float *targets, int32_t batch,
@@ -1097,6 +1170,7 @@ int msfem_surrogate_train_step(msfem_surrogate *s, const float *features, const 
   if (loss) {
     MSFEM_CUDA(cudaMemcpyAsync(loss, s->loss.ptr, sizeof(double), cudaMemcpyDeviceToHost, s->h->stream));
     MSFEM_CUDA(cudaStreamSynchronize(s->h->stream));
+    return surrogate_check(s);
   }
   return MSFEM_OK;
 }
@@ -1402,6 +1476,8 @@ int run_batch_impl(msfem_handle *h, const msfem_batch_desc *d, double *M, double
     MSFEM_CUDA(cudaMemcpyAsync(rf_h.data(), p.refinements, sizeof(int32_t) * nc, cudaMemcpyDeviceToHost, h->stream));
   }
   if (need_host) MSFEM_CUDA(cudaStreamSynchronize(h->stream));
+  if (need_host && d->warm_start == MSFEM_WARM_SURROGATE && nc > 0 && (rc = surrogate_check(h->surrogate)))
+    return rc;
   for (int c = 0; c < (int)st_h.size(); ++c) nfail += st_h[c] != MSFEM_CELL_CONVERGED;
   if (stats) {
     std::memset(stats, 0, sizeof(*stats));

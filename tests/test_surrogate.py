@@ -91,3 +91,23 @@ def test_training_reduces_loss_and_warm_start_saves_iterations(pkg, engine):
     assert np.abs(Mc - Mw).max() < 1e-9 * np.abs(Mc).max()
     assert warm["stats"]["iterations_total"] < cold["stats"]["iterations_total"]
     sur.close()
+
+
+@pytest.mark.gpu
+def test_predict_is_independent_per_image(pkg, engine):
+    """Each image's prediction depends only on that image: a large batch
+    (many work items per persistent CTA, prefetched windows, reused tensor
+    memory) equals the same images predicted on their own, bit for bit."""
+    torch = pytest.importorskip("torch")
+    sur = pkg.surrogate.Surrogate(engine, seed=11)
+    rng = np.random.default_rng(5)
+    B = 1500
+    feats = torch.from_numpy(rng.normal(0, 1, (B, 3, 33, 33)).astype(np.float32)).cuda()
+    out = torch.empty((B, 4, 33, 33), dtype=torch.float32, device="cuda")
+    sur.predict(feats, out)
+    assert torch.isfinite(out).all()
+    for lo, hi in ((0, 3), (700, 701), (B - 5, B)):
+        part = torch.empty((hi - lo, 4, 33, 33), dtype=torch.float32, device="cuda")
+        sur.predict(feats[lo:hi].contiguous(), part)
+        assert torch.equal(part, out[lo:hi])
+    sur.close()
