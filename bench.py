@@ -204,6 +204,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile", default=None, choices=["fp64_2d", "mixed_2d", "fp64_3d", "mixed_3d", "cnn"],
                     help="run one small single-kernel case (for ncu captures) and exit")
+    ap.add_argument("--variant", type=int, default=None, help="--profile 2D: launch shape index to use")
+    ap.add_argument("--inner-tol", type=float, default=1e-6, help="--profile 2D mixed: inner FP32 reduction")
+    ap.add_argument("--cheb-ratio", type=float, default=30.0, help="--profile 2D mixed: Chebyshev interval ratio")
     ap.add_argument("--no-config3", action="store_true", help="skip the 65536-cell config-3 timing")
     ap.add_argument("--no-surrogate", action="store_true", help="skip training / evaluating the warm start")
     ap.add_argument("--no-config4", action="store_true", help="skip the 3D uneven-N config-4 timing")
@@ -349,6 +352,10 @@ def main():
             # 48x48 cells: a 226 MB tabulated field, larger than L2
             wsp = make_ws(W.config2(K=48, N=N_FINE), 0)
             prec = abi.PREC_FP64 if kind == "fp64_2d" else abi.PREC_MIXED
+            if args.variant is not None:
+                eng.set_tuning({"dim": 2, "n_max": N_FINE, "precision": prec, "variant": args.variant,
+                                "check_interval": 0, "inner_tol": args.inner_tol,
+                                "cheb_ratio": args.cheb_ratio})
             t_ms, _, _ = timed_ws(wsp, prec, args.steps, args.warmup)
         elif kind in ("fp64_3d", "mixed_3d"):
             # the first 256 cells of config 4 (uneven N, 1e4-contrast spheres)
@@ -397,7 +404,18 @@ def main():
     def timed(precision, steps, warmup, sample_clocks=False):
         return timed_ws(ws2, precision, steps, warmup, sample_clocks)
 
+    def autotune_ws(ws, precision, sample=1024):
+        """The library's autotuner on a prefix of the workload (untimed); the
+        choice stays in the handle for every later call with the same key."""
+        d = device_desc(ws, precision)
+        t = abi.Tuning()
+        rc = eng.lib.msfem_autotune(eng.handle, ctypes.byref(d), sample, ctypes.byref(t))
+        if rc != abi.OK:
+            raise abi.MsfemError(rc, abi.last_error(eng.lib))
+        return t.as_dict()
+
     # ---- FP64 form (headline)
+    tune64 = autotune_ws(ws2, abi.PREC_FP64)
     ms64, st64, clocks = timed(abi.PREC_FP64, args.steps, args.warmup, sample_clocks=True)
     value = pkg.sharding.job_throughput(world * solves_rank, ms64 * 1e-3)
     probe = load_probe(pkg)
@@ -442,13 +460,15 @@ def main():
         "stats": {"mean_iterations": st64["iterations_total"] / max(1, st64["solves"]),
                   "max_iterations": st64["iterations_max"],
                   "max_rel_residual": st64["max_rel_residual"],
-                  "cells_failed": st64["cells_failed"], "ctas_per_sm": st64["ctas_per_sm"]},
+                  "cells_failed": st64["cells_failed"], "ctas_per_sm": st64["ctas_per_sm"], "tuning": tune64},
     }
     M64 = M_d.cpu().numpy().copy()
     # ---- mixed form
     if not args.no_mixed:
+        tunemx = autotune_ws(ws2, abi.PREC_MIXED)
         msmx, stmx, _ = timed(abi.PREC_MIXED, args.steps, args.warmup)
         line["mixed"] = {
+            "tuning": tunemx,
             "value": world * solves_rank / (msmx * 1e-3), "ms_per_step": msmx,
             "speedup_vs_fp64": ms64 / msmx,
             "mean_inner_iterations": stmx["iterations_total"] / max(1, stmx["solves"]),

@@ -238,6 +238,10 @@ typedef struct msfem_tuning {
   float inner_tol;          /* MIXED: inner FP32 CG relative reduction */
   int32_t n_variants;       /* output: compiled shapes for this key */
   double ms_per_solve;      /* output of msfem_autotune: device time per basis solve */
+  float cheb_ratio;         /* MIXED, polynomial-preconditioned shapes: b / a of the
+                               Chebyshev interval [a, b], b the Gershgorin bound */
+  int32_t poly_degree;      /* output: degree of that shape's polynomial preconditioner
+                               (0 = Jacobi-scaled CG) */
 } msfem_tuning;
 
 /* Time every compiled shape and parameter choice for desc's key on a prefix

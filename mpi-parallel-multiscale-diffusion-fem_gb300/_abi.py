@@ -118,6 +118,8 @@ class Tuning(ctypes.Structure):
         ("inner_tol", ctypes.c_float),
         ("n_variants", ctypes.c_int32),
         ("ms_per_solve", ctypes.c_double),
+        ("cheb_ratio", ctypes.c_float),
+        ("poly_degree", ctypes.c_int32),
     ]
 
     def as_dict(self):

@@ -41,6 +41,7 @@ struct KernelParams {
   float inner_tol;             // mixed: inner FP32 relative reduction
   int inner_maxit;             // mixed: inner iteration cap per refinement
   int max_refine;              // mixed: outer refinement cap
+  float cheb_ratio;            // mixed, polynomial-preconditioned: b / a of the Chebyshev interval
 };
 
 // The reference's pi constant (include/coefficients/coefficients.h:21).

@@ -66,6 +66,7 @@ struct Tune {
   int variant = 0;
   int check_interval = 0;
   float inner_tol = 1e-6f;
+  float cheb_ratio = 30.0f;
   double ms_per_solve = 0.0;
 };
 
@@ -294,17 +295,19 @@ struct Launch {
   int rows;          // nodes per thread strip (mixed kernels), 0 otherwise
   int minb;          // CTAs per SM the kernel was compiled for
   size_t slot_bytes; // per-CTA global workspace (3D kernels), 0 = none
+  int poly;          // degree of the inner polynomial preconditioner (mixed 2D), 0 = none
 };
 
 template <int NMAX, int NT>
 Launch make2d() {
   return Launch{(const void *)msfem::msfem2d_kernel<NMAX, NT>, NT, msfem::Smem2D<NMAX>::bytes(false),
-                0, 2, 0};
+                0, 2, 0, 0};
 }
-template <int NMAX, int NT, int S, int MINB>
+template <int NMAX, int NT, int S, int MINB, int M = 0>
 Launch make2d_mixed() {
-  return Launch{(const void *)msfem::msfem2d_mixed_kernel<NMAX, NT, S, MINB>, NT,
-                msfem::Smem2D<NMAX>::bytes(true), S, MINB, 0};
+  using L = msfem::Smem2D<NMAX>;
+  return Launch{(const void *)msfem::msfem2d_mixed_kernel<NMAX, NT, S, MINB, M>, NT,
+                M > 0 ? L::kEndCheb : L::bytes(true), S, MINB, 0, M > 0 ? M - 1 : 0};
 }
 
 // Compiled launch shapes per (dim, N class, precision); index 0 is the default.
@@ -313,13 +316,16 @@ std::vector<Launch> candidates(int dim, int nmax, bool mixed) {
     if (nmax <= 16) {
       if (mixed)
         return {make2d_mixed<16, 128, 2, 2>(), make2d_mixed<16, 64, 4, 4>(),
-                make2d_mixed<16, 128, 2, 1>()};
+                make2d_mixed<16, 128, 2, 1>(), make2d_mixed<16, 128, 2, 2, 4>()};
       return {make2d<16, 128>()};
     }
     if (nmax <= 32) {
       if (mixed)
         return {make2d_mixed<32, 256, 4, 2>(), make2d_mixed<32, 256, 4, 1>(),
-                make2d_mixed<32, 512, 2, 1>()};
+                make2d_mixed<32, 512, 2, 1>(),
+                // polynomial-preconditioned inner CG (degree M - 1 Chebyshev)
+                make2d_mixed<32, 512, 2, 1, 4>(), make2d_mixed<32, 512, 2, 1, 6>(),
+                make2d_mixed<32, 256, 4, 1, 4>(), make2d_mixed<32, 256, 4, 1, 6>()};
       return {make2d<32, 256>()};
     }
     return {};
@@ -327,11 +333,11 @@ std::vector<Launch> candidates(int dim, int nmax, bool mixed) {
   if (nmax > MSFEM_MAX_N_3D) return {};
   const size_t slot = msfem::Work3D::bytes(mixed);
   if (mixed)
-    return {Launch{(const void *)msfem::msfem3d_kernel<256, true>, 256, 0, 0, 2, slot},
-            Launch{(const void *)msfem::msfem3d_kernel<512, true>, 512, 0, 0, 1, slot},
-            Launch{(const void *)msfem::msfem3d_kernel<256, true>, 256, 0, 0, 4, slot}};
-  return {Launch{(const void *)msfem::msfem3d_kernel<256, false>, 256, 0, 0, 2, slot},
-          Launch{(const void *)msfem::msfem3d_kernel<512, false>, 512, 0, 0, 1, slot}};
+    return {Launch{(const void *)msfem::msfem3d_kernel<256, true>, 256, 0, 0, 2, slot, 0},
+            Launch{(const void *)msfem::msfem3d_kernel<512, true>, 512, 0, 0, 1, slot, 0},
+            Launch{(const void *)msfem::msfem3d_kernel<256, true>, 256, 0, 0, 4, slot, 0}};
+  return {Launch{(const void *)msfem::msfem3d_kernel<256, false>, 256, 0, 0, 2, slot, 0},
+          Launch{(const void *)msfem::msfem3d_kernel<512, false>, 512, 0, 0, 1, slot, 0}};
 }
 
 int size_class(int dim, int nmax) {
@@ -594,6 +600,7 @@ int msfem_run_batch_noalloc(const msfem_batch_desc *d, double *M, double *F, dou
   p.inner_tol = Tune().inner_tol;
   p.inner_maxit = std::max(1, std::min(d->maxit, 1000));
   p.max_refine = 40;
+  p.cheb_ratio = Tune().cheb_ratio;
   p.warm_basis = d->warm_start == MSFEM_WARM_USER ? d->warm_basis : nullptr;
   p.basis_offset = nullptr;
   p.M = M;
@@ -1344,6 +1351,7 @@ int run_batch_impl(msfem_handle *h, const msfem_batch_desc *d, double *M, double
   p.inner_tol = tn.inner_tol;
   p.inner_maxit = std::max(1, std::min(d->maxit, 1000));
   p.max_refine = 40;
+  p.cheb_ratio = tn.cheb_ratio;
   if (d->warm_start == MSFEM_WARM_USER) {
     const double *wb = nullptr;
     if ((rc = upload<double>(h, h->warm, d->warm_basis, (size_t)basis_total, dev, &wb, &h2d))) return rc;
@@ -1520,7 +1528,9 @@ void fill_tuning(const Tune &t, int dim, int nmax, int precision, msfem_tuning *
     out->threads = c[t.variant].nt;
     out->rows_per_thread = c[t.variant].rows;
     out->ctas_per_sm = c[t.variant].minb;
+    out->poly_degree = c[t.variant].poly;
   }
+  out->cheb_ratio = t.cheb_ratio;
   out->check_interval = t.check_interval;
   out->inner_tol = t.inner_tol;
   out->ms_per_solve = t.ms_per_solve;
@@ -1593,6 +1603,7 @@ int msfem_set_tuning(msfem_handle *h, const msfem_tuning *t) {
   tn.variant = t->variant;
   tn.check_interval = t->check_interval;
   tn.inner_tol = t->inner_tol;
+  tn.cheb_ratio = t->cheb_ratio > 1.0f ? t->cheb_ratio : Tune().cheb_ratio;
   tn.ms_per_solve = t->ms_per_solve;
   h->tuning[tune_key(t->dim, t->n_max, mixed)] = tn;
   return MSFEM_OK;
@@ -1636,10 +1647,20 @@ int msfem_autotune(msfem_handle *h, const msfem_batch_desc *d, int32_t sample_ce
   for (int v = 0; v < (int)cands.size(); ++v) {
     if (mixed) {
       for (float it : {1e-4f, 1e-5f, 1e-6f, 1e-7f}) {
-        Tune t;
-        t.variant = v;
-        t.inner_tol = it;
-        trials.push_back(t);
+        if (cands[v].poly > 0) {
+          for (float ratio : {10.0f, 30.0f, 100.0f}) {
+            Tune t;
+            t.variant = v;
+            t.inner_tol = it;
+            t.cheb_ratio = ratio;
+            trials.push_back(t);
+          }
+        } else {
+          Tune t;
+          t.variant = v;
+          t.inner_tol = it;
+          trials.push_back(t);
+        }
       }
     } else {
       for (int ci : {0, 1, 4}) {

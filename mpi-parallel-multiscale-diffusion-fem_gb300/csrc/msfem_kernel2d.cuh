@@ -25,6 +25,7 @@
 //   v64 [G][4]  FP64 work vector of the 4 RHS (p~ in FP64 CG, phi~ otherwise)
 //   d64 [G]     diagonal D (D^-1/2 is recomputed where needed)
 //   v32 [G][4]  FP32 search direction of the mixed inner loop
+//   v32b[G][4]  FP32 second exchange buffer (polynomial-preconditioned form)
 #pragma once
 
 #include "msfem_common.cuh"
@@ -43,6 +44,8 @@ struct Smem2D {
   static constexpr size_t kEndFP64 = al(kD64 + sizeof(double) * G);
   static constexpr size_t kV32 = kEndFP64;
   static constexpr size_t kEndMixed = al(kV32 + sizeof(float) * 4 * G);
+  static constexpr size_t kV32B = kEndMixed;  // second FP32 exchange buffer (polynomial preconditioner)
+  static constexpr size_t kEndCheb = al(kV32B + sizeof(float) * 4 * G);
   static constexpr size_t bytes(bool mixed) { return mixed ? kEndMixed : kEndFP64; }
   static_assert(kV64 % 16 == 0 && kV32 % 16 == 0, "vector alignment");
 };
@@ -860,6 +863,107 @@ msfem2d_kernel(const KernelParams p) {
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// Strip helpers of the mixed form (thread = S consecutive rows of one column)
+// ---------------------------------------------------------------------------
+// FP32 couplings of a strip row: E, W, N, S, NE, SW, NW, SE.
+template <int S>
+struct StripCoup {
+  float cE[S], cW[S], cN[S], cS[S], cNE[S], cSW[S], cNW[S], cSE[S];
+};
+
+// y = A~ x on the strip's own rows: own-column neighbours from the registers
+// x, the two neighbour columns and the two halo rows from buf ([G][4] FP32,
+// zero outside the interior).  Each value of a neighbour column is loaded
+// once and scattered into the (up to three) rows that couple to it.
+template <int S>
+__device__ __forceinline__ void strip_apply(const float *__restrict__ buf, int g0, int P, int ns,
+                                            const StripCoup<S> &c, const float (&x)[S][4], float (&y)[S][4]) {
+#pragma unroll
+  for (int s = 0; s < S; ++s)
+#pragma unroll
+    for (int r = 0; r < 4; ++r) y[s][r] = x[s][r];
+  if (ns <= 0) return;
+  float t4[4];
+  ld4(buf, g0 - P, t4);  // row below the strip
+#pragma unroll
+  for (int r = 0; r < 4; ++r) y[0][r] = fmaf(c.cS[0], t4[r], y[0][r]);
+#pragma unroll
+  for (int s = 0; s < S; ++s) {
+    if (s < ns) {
+      if (s > 0) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) y[s][r] = fmaf(c.cS[s], x[s - 1][r], y[s][r]);
+      }
+      if (s + 1 < ns) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) y[s][r] = fmaf(c.cN[s], x[s + 1][r], y[s][r]);
+      } else {
+        ld4(buf, g0 + (s + 1) * P, t4);  // row above the strip
+#pragma unroll
+        for (int r = 0; r < 4; ++r) y[s][r] = fmaf(c.cN[s], t4[r], y[s][r]);
+      }
+    }
+  }
+#pragma unroll
+  for (int t = -1; t <= S; ++t) {
+    if (t <= ns) {
+      ld4(buf, g0 + t * P - 1, t4);  // left column, row s0 + t
+      if (t >= 1 && t - 1 < ns) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) y[t - 1][r] = fmaf(c.cNW[t - 1], t4[r], y[t - 1][r]);
+      }
+      if (t >= 0 && t < ns) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) y[t][r] = fmaf(c.cW[t], t4[r], y[t][r]);
+      }
+      if (t + 1 < ns && t + 1 < S) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) y[t + 1][r] = fmaf(c.cSW[t + 1], t4[r], y[t + 1][r]);
+      }
+      ld4(buf, g0 + t * P + 1, t4);  // right column, row s0 + t
+      if (t >= 1 && t - 1 < ns) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) y[t - 1][r] = fmaf(c.cNE[t - 1], t4[r], y[t - 1][r]);
+      }
+      if (t >= 0 && t < ns) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) y[t][r] = fmaf(c.cE[t], t4[r], y[t][r]);
+      }
+      if (t + 1 < ns && t + 1 < S) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) y[t + 1][r] = fmaf(c.cSE[t + 1], t4[r], y[t + 1][r]);
+      }
+    }
+  }
+}
+
+template <int S>
+__device__ __forceinline__ void strip_store(float *__restrict__ buf, int g0, int P, int ns, const float (&x)[S][4]) {
+#pragma unroll
+  for (int s = 0; s < S; ++s)
+    if (s < ns) st4(buf, g0 + s * P, x[s]);
+}
+
+// Block sum of K FP32 values; every thread ends with the K totals.  red
+// holds NW * K floats; callers alternate two such arrays so that a sum can
+// follow the previous one without an extra barrier.
+template <int K, int NW>
+__device__ __forceinline__ void block_sum_f(float (&v)[K], float *red, int warp, int lane) {
+  const float t = warp_transpose_reduce<K>(v, lane);
+  constexpr int SPAN = 32 / K;
+  if ((lane & (SPAN - 1)) == 0) red[warp * K + lane / SPAN] = t;
+  __syncthreads();
+  float s = 0.f;
+  for (int i = lane; i < NW * K; i += 32) s += red[i];
+  // lane l now holds partial sums of value l % K
+#pragma unroll
+  for (int m = K; m < 32; m <<= 1) s += shfl_xor_d(s, m);
+#pragma unroll
+  for (int j = 0; j < K; ++j) v[j] = __shfl_sync(0xffffffffu, s, j);
+}
+
 // ===========================================================================
 // Mixed form: FP64 residual refinement around an FP32 CG.  Thread t owns
 // interior column ix = 1 + t % (N-1) and rows s0 .. s0+S-1 of it,
@@ -867,7 +971,7 @@ msfem2d_kernel(const KernelParams p) {
 // registers, only its two neighbour columns and two halo rows come from
 // shared memory.
 // ===========================================================================
-template <int NMAX, int NT, int S, int MINB>
+template <int NMAX, int NT, int S, int MINB, int M>
 __global__ void __launch_bounds__(NT, MINB)
 msfem2d_mixed_kernel(const KernelParams p) {
   using L = Smem2D<NMAX>;
@@ -879,9 +983,11 @@ msfem2d_mixed_kernel(const KernelParams p) {
   double *v64 = reinterpret_cast<double *>(smem_raw + L::kV64);
   double *d64 = reinterpret_cast<double *>(smem_raw + L::kD64);
   float *v32 = reinterpret_cast<float *>(smem_raw + L::kV32);
+  float *v32b = reinterpret_cast<float *>(smem_raw + L::kV32B);  // used only when M > 0
   __shared__ CellShared2D cs;
   __shared__ double red[2][NW * 8];
-  __shared__ float red32[2][NW * 4];
+  __shared__ float red32[2][NW * 8];
+  __shared__ float gersh_part[NW];
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
@@ -901,6 +1007,8 @@ msfem2d_mixed_kernel(const KernelParams p) {
       __syncthreads();
       continue;
     }
+    if constexpr (M > 0)
+      for (int i = tid; i < 4 * (N + 3) * (N + 3); i += NT) v32b[i] = 0.0f;
     assemble2d<NT>(p, cs, cell, N, c64, d64, tid);
     if (cs.status != MSFEM_CELL_CONVERGED) {
       cell_report_bad(p, cs, cell, tid);
@@ -967,19 +1075,46 @@ msfem2d_mixed_kernel(const KernelParams p) {
         }
     }
     // FP32 couplings of the strip: E, W, N, S, NE, SW, NW, SE of every row
-    float cE[S], cW[S], cN[S], cS[S], cNE[S], cSW[S], cNW[S], cSE[S];
+    StripCoup<S> cp;
+    float gmax = 0.0f;  // Gershgorin bound of A~ (unit diagonal) over the strip
 #pragma unroll
     for (int s = 0; s < S; ++s) {
       const int g = g0 + s * P;
       const bool v = s < ns;
-      cE[s] = v ? (float)c64[4 * g + 0] : 0.f;
-      cNE[s] = v ? (float)c64[4 * g + 1] : 0.f;
-      cN[s] = v ? (float)c64[4 * g + 2] : 0.f;
-      cNW[s] = v ? (float)c64[4 * g + 3] : 0.f;
-      cW[s] = v ? (float)c64[4 * (g - 1) + 0] : 0.f;
-      cS[s] = v ? (float)c64[4 * (g - P) + 2] : 0.f;
-      cSW[s] = v ? (float)c64[4 * (g - P - 1) + 1] : 0.f;
-      cSE[s] = v ? (float)c64[4 * (g - P + 1) + 3] : 0.f;
+      cp.cE[s] = v ? (float)c64[4 * g + 0] : 0.f;
+      cp.cNE[s] = v ? (float)c64[4 * g + 1] : 0.f;
+      cp.cN[s] = v ? (float)c64[4 * g + 2] : 0.f;
+      cp.cNW[s] = v ? (float)c64[4 * g + 3] : 0.f;
+      cp.cW[s] = v ? (float)c64[4 * (g - 1) + 0] : 0.f;
+      cp.cS[s] = v ? (float)c64[4 * (g - P) + 2] : 0.f;
+      cp.cSW[s] = v ? (float)c64[4 * (g - P - 1) + 1] : 0.f;
+      cp.cSE[s] = v ? (float)c64[4 * (g - P + 1) + 3] : 0.f;
+      gmax = fmaxf(gmax, 1.0f + fabsf(cp.cE[s]) + fabsf(cp.cW[s]) + fabsf(cp.cN[s]) + fabsf(cp.cS[s]) +
+                             fabsf(cp.cNE[s]) + fabsf(cp.cSW[s]) + fabsf(cp.cNW[s]) + fabsf(cp.cSE[s]));
+    }
+    // Chebyshev interval [b / ratio, b] of the polynomial preconditioner: b
+    // the Gershgorin bound (>= lambda_max, so the polynomial stays positive
+    // on the spectrum and the preconditioner SPD)
+    float cheb_c1[M > 0 ? M : 1], cheb_c2[M > 0 ? M : 1], cheb_inv_theta = 1.0f;
+    if constexpr (M > 0) {
+#pragma unroll
+      for (int m = 16; m >= 1; m >>= 1) gmax = fmaxf(gmax, __shfl_xor_sync(0xffffffffu, gmax, m));
+      if (lane == 0) gersh_part[warp] = gmax;
+      __syncthreads();
+      float bmax = 1.0f;
+      for (int w = 0; w < NW; ++w) bmax = fmaxf(bmax, gersh_part[w]);
+      const float amin = bmax / fmaxf(p.cheb_ratio, 1.5f);
+      const float theta = 0.5f * (bmax + amin), delta = 0.5f * (bmax - amin), sigma = theta / delta;
+      cheb_inv_theta = 1.0f / theta;
+      float rho_prev = 1.0f / sigma;
+      cheb_c1[0] = cheb_c2[0] = 0.0f;
+#pragma unroll
+      for (int k = 1; k < M; ++k) {
+        const float rho_k = 1.0f / (2.0f * sigma - rho_prev);
+        cheb_c1[k] = rho_k * rho_prev;
+        cheb_c2[k] = 2.0f * rho_k / delta;
+        rho_prev = rho_k;
+      }
     }
 
     const double tol2 = p.tol * p.tol;
@@ -1038,142 +1173,264 @@ msfem2d_mixed_kernel(const KernelParams p) {
       __syncthreads();
       if (cs.done) break;
       ++ref;
-      // ---- inner FP32 CG on A~ d = r (active RHS only)
-      float act[4];
-#pragma unroll
-      for (int r = 0; r < 4; ++r) act[r] = cs.active[r] ? 1.0f : 0.0f;
-      float rv[S][4], pv[S][4], qv[S][4], dv[S][4];
-      float rho[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-      for (int s = 0; s < S; ++s) {
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-          rv[s][r] = s < ns ? (float)r64[s][r] * act[r] : 0.0f;
-          pv[s][r] = rv[s][r];
-          dv[s][r] = 0.0f;
-          qv[s][r] = 0.0f;
-          rho[r] = fmaf(rv[s][r], rv[s][r], rho[r]);
+      float dv[S][4];
+      if constexpr (M == 0) {
+        // ---- inner FP32 CG on A~ d = r (active RHS only)
+        float act[4];
+  #pragma unroll
+        for (int r = 0; r < 4; ++r) act[r] = cs.active[r] ? 1.0f : 0.0f;
+        float rv[S][4], pv[S][4], qv[S][4];
+        float rho[4] = {0.f, 0.f, 0.f, 0.f};
+  #pragma unroll
+        for (int s = 0; s < S; ++s) {
+  #pragma unroll
+          for (int r = 0; r < 4; ++r) {
+            rv[s][r] = s < ns ? (float)r64[s][r] * act[r] : 0.0f;
+            pv[s][r] = rv[s][r];
+            dv[s][r] = 0.0f;
+            qv[s][r] = 0.0f;
+            rho[r] = fmaf(rv[s][r], rv[s][r], rho[r]);
+          }
+          if (s < ns) st4(v32, g0 + s * P, pv[s]);
         }
-        if (s < ns) st4(v32, g0 + s * P, pv[s]);
-      }
-      block_sum4(rho);
-      const float rho0[4] = {rho[0], rho[1], rho[2], rho[3]};
-      // Inner target: the fixed relative reduction, but never deeper than the
-      // outer goal needs (with a factor 10 margin): ||r|| <= 0.1 tol ||b||.
-      float itol2r[4];
-      bool iact[4];
-#pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        iact[r] = act[r] > 0.0f && rho[r] > 0.0f;
-        const double goal = cs.nu[r] > 0.0 ? 0.01 * tol2 * cs.bb[r] / cs.nu[r] : 0.0;
-        itol2r[r] = fmaxf(itol2, (float)fmin(goal, 0.25));
-      }
-      int iit = 0;
-      for (;;) {
-        if (!(iact[0] || iact[1] || iact[2] || iact[3]) || iit >= p.inner_maxit) break;
-        ++iit;
-        // q = A~ p on the strip.  Own-column neighbours come from registers
-        // (halo rows from shared memory); each value of the two neighbour
-        // columns is loaded once and scattered into the (up to three) rows
-        // that couple to it.
-        float sg[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-        for (int s = 0; s < S; ++s)
-#pragma unroll
-          for (int r = 0; r < 4; ++r) qv[s][r] = pv[s][r];
-        if (ns > 0) {
-          float t4[4];
-          ld4(v32, g0 - P, t4);  // row below the strip
-#pragma unroll
-          for (int r = 0; r < 4; ++r) qv[0][r] = fmaf(cS[0], t4[r], qv[0][r]);
-#pragma unroll
-          for (int s = 0; s < S; ++s) {
-            if (s < ns) {
-              if (s > 0) {
-#pragma unroll
-                for (int r = 0; r < 4; ++r) qv[s][r] = fmaf(cS[s], pv[s - 1][r], qv[s][r]);
+        block_sum4(rho);
+        const float rho0[4] = {rho[0], rho[1], rho[2], rho[3]};
+        // Inner target: the fixed relative reduction, but never deeper than the
+        // outer goal needs (with a factor 10 margin): ||r|| <= 0.1 tol ||b||.
+        float itol2r[4];
+        bool iact[4];
+  #pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          iact[r] = act[r] > 0.0f && rho[r] > 0.0f;
+          const double goal = cs.nu[r] > 0.0 ? 0.01 * tol2 * cs.bb[r] / cs.nu[r] : 0.0;
+          itol2r[r] = fmaxf(itol2, (float)fmin(goal, 0.25));
+        }
+        int iit = 0;
+        for (;;) {
+          if (!(iact[0] || iact[1] || iact[2] || iact[3]) || iit >= p.inner_maxit) break;
+          ++iit;
+          // q = A~ p on the strip.  Own-column neighbours come from registers
+          // (halo rows from shared memory); each value of the two neighbour
+          // columns is loaded once and scattered into the (up to three) rows
+          // that couple to it.
+          float sg[4] = {0.f, 0.f, 0.f, 0.f};
+  #pragma unroll
+          for (int s = 0; s < S; ++s)
+  #pragma unroll
+            for (int r = 0; r < 4; ++r) qv[s][r] = pv[s][r];
+          if (ns > 0) {
+            float t4[4];
+            ld4(v32, g0 - P, t4);  // row below the strip
+  #pragma unroll
+            for (int r = 0; r < 4; ++r) qv[0][r] = fmaf(cp.cS[0], t4[r], qv[0][r]);
+  #pragma unroll
+            for (int s = 0; s < S; ++s) {
+              if (s < ns) {
+                if (s > 0) {
+  #pragma unroll
+                  for (int r = 0; r < 4; ++r) qv[s][r] = fmaf(cp.cS[s], pv[s - 1][r], qv[s][r]);
+                }
+                if (s + 1 < ns) {
+  #pragma unroll
+                  for (int r = 0; r < 4; ++r) qv[s][r] = fmaf(cp.cN[s], pv[s + 1][r], qv[s][r]);
+                } else {
+                  ld4(v32, g0 + (s + 1) * P, t4);  // row above the strip
+  #pragma unroll
+                  for (int r = 0; r < 4; ++r) qv[s][r] = fmaf(cp.cN[s], t4[r], qv[s][r]);
+                }
               }
-              if (s + 1 < ns) {
-#pragma unroll
-                for (int r = 0; r < 4; ++r) qv[s][r] = fmaf(cN[s], pv[s + 1][r], qv[s][r]);
+            }
+  #pragma unroll
+            for (int t = -1; t <= S; ++t) {
+              if (t <= ns) {
+                ld4(v32, g0 + t * P - 1, t4);  // left column, row s0 + t
+                if (t >= 1 && t - 1 < ns) {
+  #pragma unroll
+                  for (int r = 0; r < 4; ++r) qv[t - 1][r] = fmaf(cp.cNW[t - 1], t4[r], qv[t - 1][r]);
+                }
+                if (t >= 0 && t < ns) {
+  #pragma unroll
+                  for (int r = 0; r < 4; ++r) qv[t][r] = fmaf(cp.cW[t], t4[r], qv[t][r]);
+                }
+                if (t + 1 < ns && t + 1 < S) {
+  #pragma unroll
+                  for (int r = 0; r < 4; ++r) qv[t + 1][r] = fmaf(cp.cSW[t + 1], t4[r], qv[t + 1][r]);
+                }
+                ld4(v32, g0 + t * P + 1, t4);  // right column, row s0 + t
+                if (t >= 1 && t - 1 < ns) {
+  #pragma unroll
+                  for (int r = 0; r < 4; ++r) qv[t - 1][r] = fmaf(cp.cNE[t - 1], t4[r], qv[t - 1][r]);
+                }
+                if (t >= 0 && t < ns) {
+  #pragma unroll
+                  for (int r = 0; r < 4; ++r) qv[t][r] = fmaf(cp.cE[t], t4[r], qv[t][r]);
+                }
+                if (t + 1 < ns && t + 1 < S) {
+  #pragma unroll
+                  for (int r = 0; r < 4; ++r) qv[t + 1][r] = fmaf(cp.cSE[t + 1], t4[r], qv[t + 1][r]);
+                }
+              }
+            }
+  #pragma unroll
+            for (int s = 0; s < S; ++s)
+  #pragma unroll
+              for (int r = 0; r < 4; ++r) sg[r] = fmaf(pv[s][r], qv[s][r], sg[r]);
+          }
+          block_sum4(sg);
+          float al[4];
+  #pragma unroll
+          for (int r = 0; r < 4; ++r) al[r] = (iact[r] && sg[r] > 0.f) ? rho[r] / sg[r] : 0.0f;
+          float rp[4] = {0.f, 0.f, 0.f, 0.f};
+  #pragma unroll
+          for (int s = 0; s < S; ++s)
+  #pragma unroll
+            for (int r = 0; r < 4; ++r) {
+              dv[s][r] = fmaf(al[r], pv[s][r], dv[s][r]);
+              rv[s][r] = fmaf(-al[r], qv[s][r], rv[s][r]);
+              rp[r] = fmaf(rv[s][r], rv[s][r], rp[r]);
+            }
+          block_sum4(rp);
+          float be[4];
+  #pragma unroll
+          for (int r = 0; r < 4; ++r) {
+            be[r] = 0.0f;
+            if (iact[r]) {
+              total_iters[r] += 1;
+              if (!(rp[r] <= itol2r[r] * rho0[r]) && isfinite(rp[r])) {
+                be[r] = rp[r] / rho[r];
+                rho[r] = rp[r];
               } else {
-                ld4(v32, g0 + (s + 1) * P, t4);  // row above the strip
-#pragma unroll
-                for (int r = 0; r < 4; ++r) qv[s][r] = fmaf(cN[s], t4[r], qv[s][r]);
+                iact[r] = false;
               }
             }
           }
+  #pragma unroll
+          for (int s = 0; s < S; ++s) {
+  #pragma unroll
+            for (int r = 0; r < 4; ++r) pv[s][r] = fmaf(be[r], pv[s][r], rv[s][r]);
+            if (s < ns) st4(v32, g0 + s * P, pv[s]);
+          }
+          __syncthreads();
+        }
+
+      } else {
+        // ---- inner FP32 CG on A~ d = r preconditioned by z = P(A~) r, the
+        // Chebyshev polynomial of degree M - 1 on [b / ratio, b] (M - 1
+        // stencils exchanged through v32b / v32 alternately, no reductions)
+        float act[4];
 #pragma unroll
-          for (int t = -1; t <= S; ++t) {
-            if (t <= ns) {
-              ld4(v32, g0 + t * P - 1, t4);  // left column, row s0 + t
-              if (t >= 1 && t - 1 < ns) {
+        for (int r = 0; r < 4; ++r) act[r] = cs.active[r] ? 1.0f : 0.0f;
+        float rv[S][4], pv[S][4], zv[S][4], ddv[S][4];
 #pragma unroll
-                for (int r = 0; r < 4; ++r) qv[t - 1][r] = fmaf(cNW[t - 1], t4[r], qv[t - 1][r]);
+        for (int s = 0; s < S; ++s)
+#pragma unroll
+          for (int r = 0; r < 4; ++r) {
+            rv[s][r] = s < ns ? (float)r64[s][r] * act[r] : 0.0f;
+            dv[s][r] = 0.0f;
+          }
+        auto apply_prec = [&]() {
+#pragma unroll
+          for (int s = 0; s < S; ++s)
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+              zv[s][r] = rv[s][r] * cheb_inv_theta;
+              ddv[s][r] = zv[s][r];
+            }
+#pragma unroll
+          for (int k = 1; k < M; ++k) {
+            float *bufk = (k & 1) ? v32b : v32;
+            strip_store<S>(bufk, g0, P, ns, zv);
+            __syncthreads();
+            float yv[S][4];
+            strip_apply<S>(bufk, g0, P, ns, cp, zv, yv);
+#pragma unroll
+            for (int s = 0; s < S; ++s)
+#pragma unroll
+              for (int r = 0; r < 4; ++r) {
+                ddv[s][r] = fmaf(cheb_c1[k], ddv[s][r], cheb_c2[k] * (rv[s][r] - yv[s][r]));
+                zv[s][r] += ddv[s][r];
               }
-              if (t >= 0 && t < ns) {
+          }
+        };
+        auto dots_rz_rr = [&](float (&out)[8]) {
 #pragma unroll
-                for (int r = 0; r < 4; ++r) qv[t][r] = fmaf(cW[t], t4[r], qv[t][r]);
-              }
-              if (t + 1 < ns && t + 1 < S) {
+          for (int j = 0; j < 8; ++j) out[j] = 0.0f;
 #pragma unroll
-                for (int r = 0; r < 4; ++r) qv[t + 1][r] = fmaf(cSW[t + 1], t4[r], qv[t + 1][r]);
-              }
-              ld4(v32, g0 + t * P + 1, t4);  // right column, row s0 + t
-              if (t >= 1 && t - 1 < ns) {
+          for (int s = 0; s < S; ++s)
 #pragma unroll
-                for (int r = 0; r < 4; ++r) qv[t - 1][r] = fmaf(cNE[t - 1], t4[r], qv[t - 1][r]);
-              }
-              if (t >= 0 && t < ns) {
+            for (int r = 0; r < 4; ++r) {
+              out[r] = fmaf(rv[s][r], zv[s][r], out[r]);
+              out[4 + r] = fmaf(rv[s][r], rv[s][r], out[4 + r]);
+            }
+          block_sum_f<8, NW>(out, red32[buf], warp, lane);
+          buf ^= 1;
+        };
+        apply_prec();
+        float rzrr[8];
+        dots_rz_rr(rzrr);
+        float rho[4], rho0[4], itol2r[4];
+        bool iact[4];
 #pragma unroll
-                for (int r = 0; r < 4; ++r) qv[t][r] = fmaf(cE[t], t4[r], qv[t][r]);
-              }
-              if (t + 1 < ns && t + 1 < S) {
+        for (int r = 0; r < 4; ++r) {
+          rho[r] = rzrr[r];
+          rho0[r] = rzrr[4 + r];
+          iact[r] = act[r] > 0.0f && rho0[r] > 0.0f && rho[r] > 0.0f;
+          const double goal = cs.nu[r] > 0.0 ? 0.01 * tol2 * cs.bb[r] / cs.nu[r] : 0.0;
+          itol2r[r] = fmaxf(itol2, (float)fmin(goal, 0.25));
+        }
 #pragma unroll
-                for (int r = 0; r < 4; ++r) qv[t + 1][r] = fmaf(cSE[t + 1], t4[r], qv[t + 1][r]);
+        for (int s = 0; s < S; ++s)
+#pragma unroll
+          for (int r = 0; r < 4; ++r) pv[s][r] = zv[s][r];
+        int iit = 0;
+        for (;;) {
+          if (!(iact[0] || iact[1] || iact[2] || iact[3]) || iit >= p.inner_maxit) break;
+          ++iit;
+          // q = A~ p (p exchanged through v32)
+          strip_store<S>(v32, g0, P, ns, pv);
+          __syncthreads();
+          float qv[S][4];
+          strip_apply<S>(v32, g0, P, ns, cp, pv, qv);
+          float sg[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+          for (int s = 0; s < S; ++s)
+#pragma unroll
+            for (int r = 0; r < 4; ++r) sg[r] = fmaf(pv[s][r], qv[s][r], sg[r]);
+          block_sum_f<4, NW>(sg, red32[buf], warp, lane);
+          buf ^= 1;
+          float al[4];
+#pragma unroll
+          for (int r = 0; r < 4; ++r) al[r] = (iact[r] && sg[r] > 0.f) ? rho[r] / sg[r] : 0.0f;
+#pragma unroll
+          for (int s = 0; s < S; ++s)
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+              dv[s][r] = fmaf(al[r], pv[s][r], dv[s][r]);
+              rv[s][r] = fmaf(-al[r], qv[s][r], rv[s][r]);
+            }
+          apply_prec();
+          dots_rz_rr(rzrr);
+          float be[4];
+#pragma unroll
+          for (int r = 0; r < 4; ++r) {
+            be[r] = 0.0f;
+            if (iact[r]) {
+              total_iters[r] += 1;
+              const float rr = rzrr[4 + r], rz = rzrr[r];
+              if (!(rr <= itol2r[r] * rho0[r]) && isfinite(rr) && rz > 0.0f && sg[r] > 0.0f) {
+                be[r] = rz / rho[r];
+                rho[r] = rz;
+              } else {
+                iact[r] = false;
               }
             }
           }
 #pragma unroll
           for (int s = 0; s < S; ++s)
 #pragma unroll
-            for (int r = 0; r < 4; ++r) sg[r] = fmaf(pv[s][r], qv[s][r], sg[r]);
+            for (int r = 0; r < 4; ++r) pv[s][r] = fmaf(be[r], pv[s][r], zv[s][r]);
         }
-        block_sum4(sg);
-        float al[4];
-#pragma unroll
-        for (int r = 0; r < 4; ++r) al[r] = (iact[r] && sg[r] > 0.f) ? rho[r] / sg[r] : 0.0f;
-        float rp[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-        for (int s = 0; s < S; ++s)
-#pragma unroll
-          for (int r = 0; r < 4; ++r) {
-            dv[s][r] = fmaf(al[r], pv[s][r], dv[s][r]);
-            rv[s][r] = fmaf(-al[r], qv[s][r], rv[s][r]);
-            rp[r] = fmaf(rv[s][r], rv[s][r], rp[r]);
-          }
-        block_sum4(rp);
-        float be[4];
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-          be[r] = 0.0f;
-          if (iact[r]) {
-            total_iters[r] += 1;
-            if (!(rp[r] <= itol2r[r] * rho0[r]) && isfinite(rp[r])) {
-              be[r] = rp[r] / rho[r];
-              rho[r] = rp[r];
-            } else {
-              iact[r] = false;
-            }
-          }
-        }
-#pragma unroll
-        for (int s = 0; s < S; ++s) {
-#pragma unroll
-          for (int r = 0; r < 4; ++r) pv[s][r] = fmaf(be[r], pv[s][r], rv[s][r]);
-          if (s < ns) st4(v32, g0 + s * P, pv[s]);
-        }
-        __syncthreads();
+        __syncthreads();  // last reads of v32 / v32b before the next writes
       }
       // ---- x~ += d (FP64), new FP64 residual r = -(A~ phi~)_I
 #pragma unroll

@@ -170,19 +170,28 @@ def test_mixed_reaches_tolerance_and_matches_fp64(pkg, engine):
     assert rel_err(b["M"], a["M"]) < 1e-9
 
 
+@pytest.mark.parametrize("n_max", [32, 16])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_every_compiled_launch_shape_gives_the_same_answer(pkg, oracle, engine, precision):
-    """Each CTA shape the autotuner can pick (and each inner tolerance) keeps parity."""
+def test_every_compiled_launch_shape_gives_the_same_answer(pkg, oracle, engine, precision, n_max):
+    """Each CTA shape the autotuner can pick (each inner tolerance and, for the
+    polynomial-preconditioned shapes, each Chebyshev interval ratio) keeps parity."""
     W = pkg.workloads
-    prob = W.subset(W.config2(K=64, N=32), [3, 1000, 2222, 4000])
+    if n_max == 32:
+        prob = W.subset(W.config2(K=64, N=32), [3, 1000, 2222, 4000])
+    else:
+        prob = W.subset(W.config1(), [0, 9, 36, 63])
     ref = oracle.run(prob, want_basis=True)
     probe = engine.autotune(prob, precision=precision, tol=1e-13, sample_cells=4)
     assert probe["n_variants"] >= 1
+    prec = 0 if precision == "fp64" else 1
     for v in range(probe["n_variants"]):
+        engine.set_tuning({"dim": 2, "n_max": n_max, "precision": prec, "variant": v, "check_interval": 0,
+                           "inner_tol": 1e-6})
         for itol in ((1e-4, 1e-6) if precision == "mixed" else (1e-6,)):
-            engine.set_tuning({"dim": 2, "n_max": 32, "precision": 0 if precision == "fp64" else 1,
-                               "variant": v, "check_interval": 0, "inner_tol": itol})
-            got = engine.run(prob, precision=precision, tol=1e-13, want_basis=True)
-            check(got, ref)
-    engine.set_tuning({"dim": 2, "n_max": 32, "precision": 0 if precision == "fp64" else 1,
-                       "variant": 0, "check_interval": 0, "inner_tol": 1e-6})
+            for ratio in (10.0, 100.0) if precision == "mixed" else (30.0,):
+                engine.set_tuning({"dim": 2, "n_max": n_max, "precision": prec, "variant": v,
+                                   "check_interval": 0, "inner_tol": itol, "cheb_ratio": ratio})
+                got = engine.run(prob, precision=precision, tol=1e-13, want_basis=True)
+                check(got, ref)
+    engine.set_tuning({"dim": 2, "n_max": n_max, "precision": prec, "variant": 0, "check_interval": 0,
+                       "inner_tol": 1e-6})
