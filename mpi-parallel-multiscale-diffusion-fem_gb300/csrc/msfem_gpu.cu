@@ -306,8 +306,10 @@ Launch make2d() {
 template <int NMAX, int NT, int S, int MINB, int M = 0>
 Launch make2d_mixed() {
   using L = msfem::Smem2D<NMAX>;
+  // the polynomial-preconditioned form needs a second exchange buffer unless
+  // it runs two CTAs per SM (one buffer, one more barrier per Chebyshev step)
   return Launch{(const void *)msfem::msfem2d_mixed_kernel<NMAX, NT, S, MINB, M>, NT,
-                M > 0 ? L::kEndCheb : L::bytes(true), S, MINB, 0, M > 0 ? M - 1 : 0};
+                (M > 0 && MINB < 2) ? L::kEndCheb : L::bytes(true), S, MINB, 0, M > 0 ? M - 1 : 0};
 }
 
 // Compiled launch shapes per (dim, N class, precision); index 0 is the default.
@@ -316,7 +318,7 @@ std::vector<Launch> candidates(int dim, int nmax, bool mixed) {
     if (nmax <= 16) {
       if (mixed)
         return {make2d_mixed<16, 128, 2, 2>(), make2d_mixed<16, 64, 4, 4>(),
-                make2d_mixed<16, 128, 2, 1>(), make2d_mixed<16, 128, 2, 2, 4>()};
+                make2d_mixed<16, 128, 2, 1>(), make2d_mixed<16, 128, 2, 1, 4>()};
       return {make2d<16, 128>()};
     }
     if (nmax <= 32) {
@@ -325,19 +327,27 @@ std::vector<Launch> candidates(int dim, int nmax, bool mixed) {
                 make2d_mixed<32, 512, 2, 1>(),
                 // polynomial-preconditioned inner CG (degree M - 1 Chebyshev)
                 make2d_mixed<32, 512, 2, 1, 4>(), make2d_mixed<32, 512, 2, 1, 6>(),
-                make2d_mixed<32, 256, 4, 1, 4>(), make2d_mixed<32, 256, 4, 1, 6>()};
+                make2d_mixed<32, 256, 4, 1, 4>(), make2d_mixed<32, 256, 4, 1, 6>(),
+                make2d_mixed<32, 256, 4, 2, 4>(), make2d_mixed<32, 256, 4, 2, 6>()};
       return {make2d<32, 256>()};
     }
     return {};
   }
   if (nmax > MSFEM_MAX_N_3D) return {};
   const size_t slot = msfem::Work3D::bytes(mixed);
+  // (threads, CTAs per SM the registers are capped for): more resident warps
+  // hide the latency of the workspace loads
   if (mixed)
-    return {Launch{(const void *)msfem::msfem3d_kernel<256, true>, 256, 0, 0, 2, slot, 0},
-            Launch{(const void *)msfem::msfem3d_kernel<512, true>, 512, 0, 0, 1, slot, 0},
-            Launch{(const void *)msfem::msfem3d_kernel<256, true>, 256, 0, 0, 4, slot, 0}};
-  return {Launch{(const void *)msfem::msfem3d_kernel<256, false>, 256, 0, 0, 2, slot, 0},
-          Launch{(const void *)msfem::msfem3d_kernel<512, false>, 512, 0, 0, 1, slot, 0}};
+    return {Launch{(const void *)msfem::msfem3d_kernel<256, true, 1>, 256, 0, 0, 1, slot, 0},
+            Launch{(const void *)msfem::msfem3d_kernel<512, true, 1>, 512, 0, 0, 1, slot, 0},
+            Launch{(const void *)msfem::msfem3d_kernel<256, true, 2>, 256, 0, 0, 2, slot, 0},
+            Launch{(const void *)msfem::msfem3d_kernel<256, true, 3>, 256, 0, 0, 3, slot, 0},
+            Launch{(const void *)msfem::msfem3d_kernel<512, true, 2>, 512, 0, 0, 2, slot, 0}};
+  return {Launch{(const void *)msfem::msfem3d_kernel<256, false, 1>, 256, 0, 0, 1, slot, 0},
+          Launch{(const void *)msfem::msfem3d_kernel<512, false, 1>, 512, 0, 0, 1, slot, 0},
+          Launch{(const void *)msfem::msfem3d_kernel<256, false, 2>, 256, 0, 0, 2, slot, 0},
+          Launch{(const void *)msfem::msfem3d_kernel<256, false, 3>, 256, 0, 0, 3, slot, 0},
+          Launch{(const void *)msfem::msfem3d_kernel<512, false, 2>, 512, 0, 0, 2, slot, 0}};
 }
 
 int size_class(int dim, int nmax) {

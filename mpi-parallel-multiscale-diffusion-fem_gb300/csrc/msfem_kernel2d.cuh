@@ -1007,7 +1007,7 @@ msfem2d_mixed_kernel(const KernelParams p) {
       __syncthreads();
       continue;
     }
-    if constexpr (M > 0)
+    if constexpr (M > 0 && MINB < 2)
       for (int i = tid; i < 4 * (N + 3) * (N + 3); i += NT) v32b[i] = 0.0f;
     assemble2d<NT>(p, cs, cell, N, c64, d64, tid);
     if (cs.status != MSFEM_CELL_CONVERGED) {
@@ -1338,7 +1338,11 @@ msfem2d_mixed_kernel(const KernelParams p) {
             }
 #pragma unroll
           for (int k = 1; k < M; ++k) {
-            float *bufk = (k & 1) ? v32b : v32;
+            // two buffers alternate (one barrier per step); with one buffer
+            // (MINB >= 2, less shared memory) a second barrier orders the
+            // reads of step k before the writes of step k + 1
+            float *bufk = (MINB >= 2 || (k & 1) == 0) ? v32 : v32b;
+            if (MINB >= 2 && k > 1) __syncthreads();
             strip_store<S>(bufk, g0, P, ns, zv);
             __syncthreads();
             float yv[S][4];

@@ -293,8 +293,8 @@ __device__ void cell_geometry3d(const KernelParams &p, CellShared3D &cs, int cel
   __syncthreads();
 }
 
-template <int NT, bool MIXED>
-__global__ void __launch_bounds__(NT)
+template <int NT, bool MIXED, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
 msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t slot_bytes) {
   constexpr int NW = NT / 32;
   __shared__ CellShared3D cs;

@@ -79,3 +79,28 @@ def test_fp64_iterations_match_oracle_jacobi_pcg_3d(pkg, oracle, engine):
     got = engine.run(prob, precision="fp64", tol=1e-10, check_interval=1)
     ref = oracle.run(prob, solver=oracle.SOLVER_JACOBI_CG, tol=1e-10)
     assert np.abs(got["iters"] - ref["iters"]).max() <= 2
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_every_compiled_launch_shape_gives_the_same_answer_3d(pkg, oracle, engine, precision):
+    """Each 3D launch shape the autotuner can pick (threads x CTAs per SM,
+    i.e. register caps) keeps parity on an uneven-N, 1e4-contrast batch."""
+    W = pkg.workloads
+    rng = np.random.default_rng(9)
+    sp = np.column_stack([rng.uniform(0, 1, (400, 3)), rng.uniform(0.02, 0.05, 400)])
+    corners = W.unit_cube_corners(3, 4)[[1, 22, 40]]
+    nf = np.array([6, 9, 4], dtype=np.int32)
+    prob = W.problem(3, corners, nf, {"kind": 4, "params": [1e4], "spheres": sp})
+    ref = oracle.run(prob, want_basis=True)
+    probe = engine.autotune(prob, precision=precision, tol=1e-12, sample_cells=3)
+    prec = 0 if precision == "fp64" else 1
+    assert probe["n_variants"] >= 2
+    for v in range(probe["n_variants"]):
+        engine.set_tuning({"dim": 3, "n_max": 9, "precision": prec, "variant": v, "check_interval": 0,
+                           "inner_tol": 1e-6})
+        got = engine.run(prob, precision=precision, tol=1e-12, want_basis=True)
+        assert got["rc"] == 0 and np.all(got["status"] == 0), v
+        assert rel_err(got["M"], ref["M"]) < 1e-9, v
+        assert np.abs(got["basis"] - ref["basis"]).max() < 1e-8, v
+    engine.set_tuning({"dim": 3, "n_max": 9, "precision": prec, "variant": 0, "check_interval": 0,
+                       "inner_tol": 1e-6})
