@@ -242,6 +242,8 @@ typedef struct msfem_tuning {
                                Chebyshev interval [a, b], b the Gershgorin bound */
   int32_t poly_degree;      /* output: degree of that shape's polynomial preconditioner
                                (0 = Jacobi-scaled CG) */
+  int32_t cluster_ctas;     /* output: CTAs of a thread-block cluster sharing one cell
+                               (3D cluster shapes), 1 = one CTA per cell */
 } msfem_tuning;
 
 /* Time every compiled shape and parameter choice for desc's key on a prefix

@@ -120,6 +120,7 @@ class Tuning(ctypes.Structure):
         ("ms_per_solve", ctypes.c_double),
         ("cheb_ratio", ctypes.c_float),
         ("poly_degree", ctypes.c_int32),
+        ("cluster_ctas", ctypes.c_int32),
     ]
 
     def as_dict(self):

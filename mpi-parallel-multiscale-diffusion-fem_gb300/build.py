@@ -52,14 +52,39 @@ def _sources(folder, exts):
     return sorted(out)
 
 
+# translation units of libmsfem_gpu.so, compiled in parallel then linked
+GPU_UNITS = ["msfem_gpu.cu", "k2d.cu", "k3d_fp64.cu", "k3d_mixed.cu", "cnn_tc.cu"]
+
+
 def build_gpu(force=False, quiet=True, extra=()):
     os.makedirs(LIB_DIR, exist_ok=True)
+    obj_dir = os.path.join(LIB_DIR, "obj")
+    os.makedirs(obj_dir, exist_ok=True)
     target = os.path.join(LIB_DIR, "libmsfem_gpu.so")
-    deps = [f for f in _sources(CSRC, (".cu", ".cuh", ".h")) if not f.endswith("probe.cu")]
-    deps += [os.path.join(INCLUDE, "msfem_gpu.h")]
-    if force or _stale(target, deps):
-        cmd = [_nvcc(), *ARCH, *NVCC_FLAGS, *extra, "-I", INCLUDE, "-I", CSRC,
-               "-o", target + ".tmp", os.path.join(CSRC, "msfem_gpu.cu")]
+    headers = [f for f in _sources(CSRC, (".cuh", ".h"))] + [os.path.join(INCLUDE, "msfem_gpu.h")]
+    procs, objs = [], []
+    for unit in GPU_UNITS:
+        src = os.path.join(CSRC, unit)
+        obj = os.path.join(obj_dir, unit.replace(".cu", ".o"))
+        objs.append(obj)
+        if force or _stale(obj, [src] + headers):
+            cmd = [_nvcc(), *ARCH, *[f for f in NVCC_FLAGS if f != "-shared"], *extra, "-I", INCLUDE,
+                   "-I", CSRC, "-c", "-o", obj + ".tmp", src]
+            procs.append((cmd, obj, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.PIPE,
+                                                     text=True)))
+    errors = []
+    for cmd, obj, pr in procs:
+        out, err = pr.communicate()
+        if pr.returncode != 0:
+            errors.append(" ".join(cmd) + "\n" + out + err)
+        else:
+            os.replace(obj + ".tmp", obj)
+            if not quiet and err.strip():
+                print(err)
+    if errors:
+        raise RuntimeError("build failed:\n" + "\n".join(errors))
+    if force or procs or _stale(target, objs):
+        cmd = [_nvcc(), *ARCH, "-shared", "-o", target + ".tmp", *objs]
         _run(cmd, quiet)
         os.replace(target + ".tmp", target)
     return target

@@ -134,7 +134,7 @@ constexpr size_t wgrad_smem(int dil) {
 // Pack the FP32 parameters of layer l into the BF16 forward layout
 // [COUTp][9][CINp] and the transposed, tap-flipped layout [CINp][9][COUTp]
 // used by the input-gradient pass.
-__global__ void pack_layer_kernel(const float *__restrict__ params, int layer, __nv_bfloat16 *__restrict__ wf,
+static __global__ void pack_layer_kernel(const float *__restrict__ params, int layer, __nv_bfloat16 *__restrict__ wf,
                                   __nv_bfloat16 *__restrict__ wt, float *__restrict__ bias_pad) {
   const int cin = real_ch(layer), cout = real_ch(layer + 1);
   const int cinp = pad_ch(layer), coutp = pad_ch(layer + 1);
@@ -154,7 +154,7 @@ __global__ void pack_layer_kernel(const float *__restrict__ params, int layer, _
 
 // Features NCHW FP32 [B][3][33][33] -> channel-blocked BF16 [B][2][33][33][8]
 // (16 channels, 3 used).
-__global__ void features_to_blocked_kernel(const float *__restrict__ f, int B, __nv_bfloat16 *__restrict__ x) {
+static __global__ void features_to_blocked_kernel(const float *__restrict__ f, int B, __nv_bfloat16 *__restrict__ x) {
   const long total = (long)B * kPix;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
     const long b = i / kPix, p = i % kPix;
@@ -168,7 +168,7 @@ __global__ void features_to_blocked_kernel(const float *__restrict__ f, int B, _
 
 // MSE loss over interior nodes and its gradient (channel-blocked BF16
 // [B][2][33][33][8], 16 channels, 4 used).
-__global__ void mse_loss_kernel(const float *__restrict__ pred, const float *__restrict__ tgt, int B,
+static __global__ void mse_loss_kernel(const float *__restrict__ pred, const float *__restrict__ tgt, int B,
                                 float scale, __nv_bfloat16 *__restrict__ g, double *__restrict__ loss) {
   const long total = (long)B * kPix;
   double part = 0.0;
@@ -195,7 +195,7 @@ __global__ void mse_loss_kernel(const float *__restrict__ pred, const float *__r
 }
 
 // Adam (FP32 master weights).
-__global__ void adam_kernel(float *__restrict__ w, const float *__restrict__ gw, float *__restrict__ m,
+static __global__ void adam_kernel(float *__restrict__ w, const float *__restrict__ gw, float *__restrict__ m,
                             float *__restrict__ v, long n, float lr, float b1, float b2, float eps,
                             float bc1, float bc2) {
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {

@@ -82,6 +82,30 @@ __device__ __forceinline__ T warp_transpose_reduce(T (&v)[K], int lane) {
   return s;
 }
 
+// Warp 0 finishes a K-value block reduction: red holds NW*K warp partials
+// ([warp][value]); on return lane l holds the block total of value l % K.
+template <int K, typename T>
+__device__ __forceinline__ T warp_finish(const T *red, int NW, int lane) {
+  T s = T(0);
+  for (int i = lane; i < NW * K; i += 32) s += red[i];
+#pragma unroll
+  for (int m = K; m < 32; m <<= 1) s += shfl_xor_d(s, m);
+  return s;
+}
+
+// Per-warp partials of a K-value reduction into red[warp][K].
+template <int K, typename T>
+__device__ __forceinline__ void warp_partials(T (&vals)[K], T *red, int warp, int lane) {
+  const T tot = warp_transpose_reduce<K>(vals, lane);
+  constexpr int SPAN = 32 / K;
+  if ((lane & (SPAN - 1)) == 0) red[warp * K + lane / SPAN] = tot;
+}
+
+// QGauss(2) point i in [0,1] (reference coordinate of the two-point rule).
+__device__ __forceinline__ double gauss2(int i) {
+  return i ? 0.78867513459481288225457439025098 : 0.21132486540518711774542560974902;
+}
+
 // Lane that holds value index `vi` of a K-value transpose-reduce.
 template <int K>
 __device__ __forceinline__ int transpose_reduce_lane(int vi) { return vi * (32 / K); }

@@ -18,11 +18,9 @@
 #include <cuda_runtime.h>
 
 #include "msfem_common.cuh"
-#include "msfem_kernel2d.cuh"
-#include "msfem_kernel3d.cuh"
 #include "msfem_cnn.cuh"
-#include "msfem_conv_tc.cuh"
 #include "msfem_gpu.h"
+#include "msfem_launch.h"
 
 namespace {
 
@@ -286,68 +284,13 @@ int upload(msfem_handle *h, DevBuf &buf, const T *src, size_t count, bool device
   return MSFEM_OK;
 }
 
-// Kernel selection.  NMAX is the largest N of the batch rounded up to a
-// compiled size class.
-struct Launch {
-  const void *fn;
-  int nt;
-  size_t smem;
-  int rows;          // nodes per thread strip (mixed kernels), 0 otherwise
-  int minb;          // CTAs per SM the kernel was compiled for
-  size_t slot_bytes; // per-CTA global workspace (3D kernels), 0 = none
-  int poly;          // degree of the inner polynomial preconditioner (mixed 2D), 0 = none
-};
-
-template <int NMAX, int NT>
-Launch make2d() {
-  return Launch{(const void *)msfem::msfem2d_kernel<NMAX, NT>, NT, msfem::Smem2D<NMAX>::bytes(false),
-                0, 2, 0, 0};
-}
-template <int NMAX, int NT, int S, int MINB, int M = 0>
-Launch make2d_mixed() {
-  using L = msfem::Smem2D<NMAX>;
-  // the polynomial-preconditioned form needs a second exchange buffer unless
-  // it runs two CTAs per SM (one buffer, one more barrier per Chebyshev step)
-  return Launch{(const void *)msfem::msfem2d_mixed_kernel<NMAX, NT, S, MINB, M>, NT,
-                (M > 0 && MINB < 2) ? L::kEndCheb : L::bytes(true), S, MINB, 0, M > 0 ? M - 1 : 0};
-}
+using msfem::Launch;
 
 // Compiled launch shapes per (dim, N class, precision); index 0 is the default.
 std::vector<Launch> candidates(int dim, int nmax, bool mixed) {
-  if (dim == 2) {
-    if (nmax <= 16) {
-      if (mixed)
-        return {make2d_mixed<16, 128, 2, 2>(), make2d_mixed<16, 64, 4, 4>(),
-                make2d_mixed<16, 128, 2, 1>(), make2d_mixed<16, 128, 2, 1, 4>()};
-      return {make2d<16, 128>()};
-    }
-    if (nmax <= 32) {
-      if (mixed)
-        return {make2d_mixed<32, 256, 4, 2>(), make2d_mixed<32, 256, 4, 1>(),
-                make2d_mixed<32, 512, 2, 1>(),
-                // polynomial-preconditioned inner CG (degree M - 1 Chebyshev)
-                make2d_mixed<32, 512, 2, 1, 4>(), make2d_mixed<32, 512, 2, 1, 6>(),
-                make2d_mixed<32, 256, 4, 1, 4>(), make2d_mixed<32, 256, 4, 1, 6>(),
-                make2d_mixed<32, 256, 4, 2, 4>(), make2d_mixed<32, 256, 4, 2, 6>()};
-      return {make2d<32, 256>()};
-    }
-    return {};
-  }
+  if (dim == 2) return nmax <= MSFEM_MAX_N_2D ? msfem::candidates_2d(nmax, mixed) : std::vector<Launch>{};
   if (nmax > MSFEM_MAX_N_3D) return {};
-  const size_t slot = msfem::Work3D::bytes(mixed);
-  // (threads, CTAs per SM the registers are capped for): more resident warps
-  // hide the latency of the workspace loads
-  if (mixed)
-    return {Launch{(const void *)msfem::msfem3d_kernel<256, true, 1>, 256, 0, 0, 1, slot, 0},
-            Launch{(const void *)msfem::msfem3d_kernel<512, true, 1>, 512, 0, 0, 1, slot, 0},
-            Launch{(const void *)msfem::msfem3d_kernel<256, true, 2>, 256, 0, 0, 2, slot, 0},
-            Launch{(const void *)msfem::msfem3d_kernel<256, true, 3>, 256, 0, 0, 3, slot, 0},
-            Launch{(const void *)msfem::msfem3d_kernel<512, true, 2>, 512, 0, 0, 2, slot, 0}};
-  return {Launch{(const void *)msfem::msfem3d_kernel<256, false, 1>, 256, 0, 0, 1, slot, 0},
-          Launch{(const void *)msfem::msfem3d_kernel<512, false, 1>, 512, 0, 0, 1, slot, 0},
-          Launch{(const void *)msfem::msfem3d_kernel<256, false, 2>, 256, 0, 0, 2, slot, 0},
-          Launch{(const void *)msfem::msfem3d_kernel<256, false, 3>, 256, 0, 0, 3, slot, 0},
-          Launch{(const void *)msfem::msfem3d_kernel<512, false, 2>, 512, 0, 0, 2, slot, 0}};
+  return mixed ? msfem::candidates_3d_mixed() : msfem::candidates_3d_fp64();
 }
 
 int size_class(int dim, int nmax) {
@@ -834,74 +777,14 @@ namespace {
 using bf16 = __nv_bfloat16;
 namespace cn = msfem::cnn;
 
-// cuTensorMapEncodeTiled from the driver (no link-time dependency on libcuda).
-using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
-                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
-                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-EncodeTiledFn tensor_map_encoder() {
-  static EncodeTiledFn fn = nullptr;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    void *p = nullptr;
-    cudaDriverEntryPointQueryResult q{};
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<EncodeTiledFn>(p);
-  });
-  return fn;
-}
-
-// One 3x3 convolution layer on the tcgen05 tensor cores: X (channel-blocked
-// bf16) through a TMA tensor map (one box of (33 + 2 dil) pixels x the window
-// rows per 8-channel block), persistent CTAs capped so that their TMEM
-// columns fit the SM's 512.
+// One 3x3 convolution layer on the tcgen05 tensor cores (cnn_tc.cu).
 template <int CIN, int COUT, int EPI>
 int launch_conv(msfem_surrogate *s, int B, const bf16 *X, const bf16 *W, const float *bias, const bf16 *mask,
                 void *out, int cout_real, int dil) {
-  if (B <= 0) return MSFEM_OK;
-  const EncodeTiledFn enc = tensor_map_encoder();
-  if (!enc) return fail(MSFEM_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
-  const cn::tc::ConvGeom g = cn::tc::conv_geom(dil);
-  // blocked layout [B][CIN/8][33][33][8] viewed as 8-byte elements: dims (66
-  // per row = 33 pixels x 2, 33 rows, B * CIN/8 blocks); a box row is a
-  // contiguous run of wp pixels (2 wp elements <= 98, within the 256 limit).
-  // Two maps: boxes of kBoxRows rows and one of the remaining window rows.
-  const cuuint64_t dims[3] = {2u * cn::kW, (cuuint64_t)cn::kH, (cuuint64_t)B * (CIN / 8)};
-  const cuuint64_t strides[2] = {(cuuint64_t)cn::kW * 16, (cuuint64_t)cn::kPix * 16};
-  const cuuint32_t estr[3] = {1u, 1u, 1u};
-  const int rem = g.box_rows % cn::tc::kBoxRows;
-  CUtensorMap maps[2];
-  for (int m = 0; m < 2; ++m) {
-    const cuuint32_t rows = m == 0 ? (cuuint32_t)cn::tc::kBoxRows : (cuuint32_t)std::max(rem, 1);
-    const cuuint32_t box[3] = {2u * (cuuint32_t)g.wp, rows, 1u};
-    const CUresult r = enc(&maps[m], CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, const_cast<bf16 *>(X), dims, strides, box,
-                           estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS)
-      return fail(MSFEM_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
-  }
-  auto fn = cn::tc::conv3x3_tc_kernel<CIN, COUT, EPI>;
-  const size_t smem = cn::tc::conv_tc_smem<CIN, COUT>(dil);
-  MSFEM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)cn::tc::conv_tc_smem<CIN, COUT>(cn::kMaxDil)));
-  // all of the unified L1/shared storage as shared memory, so that several
-  // CTAs fit from the first launch on
-  MSFEM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                  (int)cudaSharedmemCarveoutMaxShared));
-  // CTAs per SM from the shared-memory capacity and the 512 TMEM columns
-  // (an SM never holds more accumulator sets than fit)
-  int smem_sm = 0, smem_rsv = 0;
-  MSFEM_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, s->h->device));
-  MSFEM_CUDA(cudaDeviceGetAttribute(&smem_rsv, cudaDevAttrReservedSharedMemoryPerBlock, s->h->device));
-  int per_sm = smem_sm / (int)(smem + smem_rsv + 256);  // + static shared memory (<= 208 B)
-  per_sm = std::min(per_sm, 512 / (cn::tc::kStages * cn::tc::kTiles * COUT));
-  if (per_sm < 1) return fail(MSFEM_ERR_UNSUPPORTED, "tensor-core convolution does not fit on an SM");
-  const long items = (long)B * g.segs;
-  const int grid = (int)std::min<long>(items, (long)per_sm * s->h->sm_count);
-  fn<<<grid, cn::tc::kThreads, smem, s->h->stream>>>(maps[0], maps[1], W, bias, mask, out, cout_real, dil, B,
-                                                      s->tc_err.as<int>());
-  MSFEM_CUDA(cudaGetLastError());
-  return MSFEM_OK;
+  const cn::ConvCtx ctx{s->h->stream, s->h->device, s->h->sm_count, s->tc_err.as<int>()};
+  std::string msg;
+  const int rc = cn::conv_tc(ctx, CIN, COUT, EPI, B, X, W, bias, mask, out, cout_real, dil, &msg);
+  return rc ? fail(rc, msg) : MSFEM_OK;
 }
 
 // After a synchronisation: report (and clear) a timeout of the tensor-core
@@ -1399,13 +1282,42 @@ int run_batch_impl(msfem_handle *h, const msfem_batch_desc *d, double *M, double
   MSFEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, L.fn, L.nt, L.smem));
   if (per_sm < 1) return fail(MSFEM_ERR_UNSUPPORTED, "kernel does not fit on an SM");
   if (L.slot_bytes) per_sm = std::min(per_sm, L.minb);  // workspace slots per SM
-  const int grid = std::max(1, std::min(nc, per_sm * h->sm_count));
+  int grid = std::max(1, std::min(nc, per_sm * h->sm_count));
+  int slots = grid;
+  // thread-block clusters: as many co-resident clusters as the GPU holds,
+  // one cell and one workspace slot per cluster
+  cudaLaunchConfig_t ccfg = {};
+  cudaLaunchAttribute cattr[1];
+  if (L.cluster > 1) {
+    if (L.cluster > 8)
+      MSFEM_CUDA(cudaFuncSetAttribute(L.fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    ccfg.gridDim = dim3(L.cluster);
+    ccfg.blockDim = dim3(L.nt);
+    ccfg.dynamicSmemBytes = L.smem;
+    ccfg.stream = h->stream;
+    cattr[0].id = cudaLaunchAttributeClusterDimension;
+    cattr[0].val.clusterDim.x = L.cluster;
+    cattr[0].val.clusterDim.y = 1;
+    cattr[0].val.clusterDim.z = 1;
+    ccfg.attrs = cattr;
+    ccfg.numAttrs = 1;
+    int ncl = 0;
+    MSFEM_CUDA(cudaOccupancyMaxActiveClusters(&ncl, L.fn, &ccfg));
+    if (ncl < 1) return fail(MSFEM_ERR_UNSUPPORTED, "no cluster of this shape fits the GPU");
+    slots = std::max(1, std::min(nc, ncl));
+    grid = slots * L.cluster;
+    ccfg.gridDim = dim3(grid);
+  }
   unsigned char *work = nullptr;
   size_t slot_bytes = L.slot_bytes;
   if (slot_bytes) {
-    MSFEM_CUDA(h->work.ensure(slot_bytes * grid));
+    MSFEM_CUDA(h->work.ensure(slot_bytes * slots));
     work = h->work.as<unsigned char>();
   }
+  auto launch_basis = [&](void **args) -> cudaError_t {
+    if (L.cluster > 1) return cudaLaunchKernelExC(&ccfg, L.fn, args);
+    return cudaLaunchKernel(L.fn, dim3(grid), dim3(L.nt), args, L.smem, h->stream);
+  };
   // Device-resident asynchronous calls replay a CUDA graph of the
   // queue-reset + basis-kernel sequence; it is re-captured whenever the
   // launch parameters (pointers, sizes, tuning) change.
@@ -1430,7 +1342,7 @@ int run_batch_impl(msfem_handle *h, const msfem_batch_desc *d, double *M, double
       cudaError_t e1 = cudaMemsetAsync(p.queue, 0, sizeof(unsigned int), h->stream);
       void *a2[] = {&p};
       void *a3[] = {&p, &work, &slot_bytes};
-      cudaError_t e2 = cudaLaunchKernel(L.fn, dim3(grid), dim3(L.nt), slot_bytes ? a3 : a2, L.smem, h->stream);
+      cudaError_t e2 = launch_basis(slot_bytes ? a3 : a2);
       cudaError_t e3 = cudaStreamEndCapture(h->stream, &graph);
       if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
         if (graph) cudaGraphDestroy(graph);
@@ -1453,7 +1365,7 @@ int run_batch_impl(msfem_handle *h, const msfem_batch_desc *d, double *M, double
     if (nc > 0) {
       void *args2[] = {&p};
       void *args3[] = {&p, &work, &slot_bytes};
-      MSFEM_CUDA(cudaLaunchKernel(L.fn, dim3(grid), dim3(L.nt), slot_bytes ? args3 : args2, L.smem, h->stream));
+      MSFEM_CUDA(launch_basis(slot_bytes ? args3 : args2));
       launches++;
     }
   }
@@ -1539,6 +1451,7 @@ void fill_tuning(const Tune &t, int dim, int nmax, int precision, msfem_tuning *
     out->rows_per_thread = c[t.variant].rows;
     out->ctas_per_sm = c[t.variant].minb;
     out->poly_degree = c[t.variant].poly;
+    out->cluster_ctas = c[t.variant].cluster;
   }
   out->cheb_ratio = t.cheb_ratio;
   out->check_interval = t.check_interval;
@@ -1585,13 +1498,11 @@ int msfem_energy_error(msfem_handle *h, const msfem_batch_desc *d, const double 
     e = h->M.as<double>();
     n = h->F.as<double>();
   }
-  constexpr int NT = 256;
   const int grid = std::max(1, std::min(nc, 4 * h->sm_count));
   if (d->dim == 2)
-    msfem::msfem2d_energy_kernel<NT><<<grid, NT, 0, h->stream>>>(p, a, r, e, n);
+    MSFEM_CUDA(msfem::launch_energy_2d(grid, h->stream, p, a, r, e, n));
   else
-    msfem::msfem3d_energy_kernel<NT><<<grid, NT, 0, h->stream>>>(p, a, r, e, n);
-  MSFEM_CUDA(cudaGetLastError());
+    MSFEM_CUDA(msfem::launch_energy_3d(grid, h->stream, p, a, r, e, n));
   if (!dev) {
     MSFEM_CUDA(cudaMemcpyAsync(err, e, sizeof(double) * nc * nv, cudaMemcpyDeviceToHost, h->stream));
     MSFEM_CUDA(cudaMemcpyAsync(ref_norm, n, sizeof(double) * nc * nv, cudaMemcpyDeviceToHost, h->stream));

@@ -92,25 +92,6 @@ __device__ __forceinline__ void stencil9(const T *__restrict__ c, const T *__res
 #undef MSFEM_ACC
 }
 
-// Warp 0 finishes a K-value block reduction: red holds NW*K warp partials
-// ([warp][value]); on return lane l holds the block total of value l % K.
-template <int K, typename T>
-__device__ __forceinline__ T warp_finish(const T *red, int NW, int lane) {
-  T s = T(0);
-  for (int i = lane; i < NW * K; i += 32) s += red[i];
-#pragma unroll
-  for (int m = K; m < 32; m <<= 1) s += shfl_xor_d(s, m);
-  return s;
-}
-
-// Per-warp partials of a K-value reduction into red[warp][K].
-template <int K, typename T>
-__device__ __forceinline__ void warp_partials(T (&vals)[K], T *red, int warp, int lane) {
-  const T tot = warp_transpose_reduce<K>(vals, lane);
-  constexpr int SPAN = 32 / K;
-  if ((lane & (SPAN - 1)) == 0) red[warp * K + lane / SPAN] = tot;
-}
-
 // Block-uniform scalars of one cell, in shared memory.
 struct CellShared2D {
   double corners[8];
@@ -144,9 +125,6 @@ __device__ __forceinline__ void bilinear_map(const double *cr, double tx, double
 }
 
 // QGauss(2) on [0,1]: (1 -+ 1/sqrt(3))/2
-__device__ __forceinline__ double gauss2(int i) {
-  return i ? 0.78867513459481288225457439025098 : 0.21132486540518711774542560974902;
-}
 // l_b(gauss2(qb)),  l_0(t) = 1 - t,  l_1(t) = t
 __device__ __forceinline__ double lval(int b, int qb) {
   return b ? gauss2(qb) : gauss2(1 - qb);
@@ -218,7 +196,7 @@ __device__ int cell_begin(const KernelParams &p, CellShared2D &cs, int cell, int
 }
 
 // Malformed cell: NaN outputs and the status word, then move on.
-__device__ void cell_report_bad(const KernelParams &p, const CellShared2D &cs, int cell, int tid) {
+__device__ inline void cell_report_bad(const KernelParams &p, const CellShared2D &cs, int cell, int tid) {
   if (tid < 16) p.M[(int64_t)cell * 16 + tid] = qnan();
   if (tid < 4) {
     p.F[(int64_t)cell * 4 + tid] = qnan();
@@ -447,7 +425,7 @@ __device__ __forceinline__ void boundary_value(const CellShared2D &cs, const dou
 // Load vector b_k = f int psi_k at node (ix, iy).  Affine cells: every fine
 // cell carries f |det| / 4 to each of its vertices; general cells: QGauss(2)
 // over the adjacent fine cells.
-__device__ double node_load(const KernelParams &p, const CellShared2D &cs, int N, int ix, int iy) {
+__device__ inline double node_load(const KernelParams &p, const CellShared2D &cs, int N, int ix, int iy) {
   if (cs.affine) {
     const double m = (ix == 0 || ix == N ? 1.0 : 2.0) * (iy == 0 || iy == N ? 1.0 : 2.0);
     return p.f_value * 0.25 * cs.absdet * m;

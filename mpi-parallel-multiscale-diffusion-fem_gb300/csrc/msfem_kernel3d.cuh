@@ -22,6 +22,8 @@
 // the forward couplings of the neighbours.
 #pragma once
 
+#include <cooperative_groups.h>
+
 #include "msfem_common.cuh"
 
 namespace msfem {
@@ -125,7 +127,7 @@ __device__ __forceinline__ int tri_index(int i, int j) {  // i <= j < 8
 }
 
 // Element matrix (upper triangle, 36 entries) of fine cell (cx,cy,cz).
-__device__ bool element3d(const KernelParams &p, const CellShared3D &cs, const double *__restrict__ tab,
+__device__ inline bool element3d(const KernelParams &p, const CellShared3D &cs, const double *__restrict__ tab,
                           int N, int cx, int cy, int cz, bool scalar, bool need_x, double (&K)[36]) {
   const int nfc = N * N * N, fc = cx + N * (cy + N * cz);
 #pragma unroll
@@ -293,25 +295,70 @@ __device__ void cell_geometry3d(const KernelParams &p, CellShared3D &cs, int cel
   __syncthreads();
 }
 
-template <int NT, bool MIXED, int MINB>
+// ---------------------------------------------------------------------------
+// Thread-block clusters: CS CTAs share one cell (CS = 1: one CTA per cell).
+// The cluster's CTAs split every node loop, meet at cluster barriers (release /
+// acquire at cluster scope, so workspace writes before a barrier are seen
+// after it), and sum reduction partials read from each other's shared memory
+// in a fixed rank order, so all CTAs take the same decisions.
+// ---------------------------------------------------------------------------
+template <int CS>
+__device__ __forceinline__ int cluster_rank() {
+  if constexpr (CS > 1) return (int)cooperative_groups::this_cluster().block_rank();
+  else return 0;
+}
+template <int CS>
+__device__ __forceinline__ void csync() {
+  if constexpr (CS > 1) cooperative_groups::this_cluster().sync();
+  else __syncthreads();
+}
+// The same shared-memory object in CTA `rank` of the cluster.
+template <int CS, typename T>
+__device__ __forceinline__ T *peer(T *ptr, int rank) {
+  if constexpr (CS > 1) return cooperative_groups::this_cluster().map_shared_rank(ptr, rank);
+  else return ptr;
+}
+
+template <int NT, bool MIXED, int MINB, int CS>
 __global__ void __launch_bounds__(NT, MINB)
 msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t slot_bytes) {
   constexpr int NW = NT / 32;
+  constexpr int CNT = NT * CS;  // threads working on one cell (the cluster's)
   __shared__ CellShared3D cs;
   __shared__ double red[2][NW * 16];
   __shared__ double redE[NW * 32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  unsigned char *slot = work + (size_t)blockIdx.x * slot_bytes;
+  const int crank = cluster_rank<CS>();  // this CTA's rank in its cluster
+  const int ctid = crank * NT + tid;     // thread index within the cluster
+  // one workspace slot per cluster
+  unsigned char *slot = work + (size_t)(blockIdx.x / CS) * slot_bytes;
+  // every CTA of the cluster ends with the same cell status (the first
+  // non-converged one in rank order)
+  auto agree_status = [&]() {
+    if constexpr (CS > 1) {
+      csync<CS>();
+      int st = MSFEM_CELL_CONVERGED;
+      if (tid == 0)
+        for (int c = 0; c < CS; ++c) {
+          const int s2 = *peer<CS>(&cs.status, c);
+          if (st == MSFEM_CELL_CONVERGED) st = s2;
+        }
+      csync<CS>();
+      if (tid == 0) cs.status = st;
+      __syncthreads();
+    }
+  };
   double *W64 = reinterpret_cast<double *>(slot);
   float *W32 = reinterpret_cast<float *>(slot + sizeof(double) * Work3D::kEnd64);
 
   for (;;) {
-    if (tid == 0) {
+    if (tid == 0 && crank == 0) {
       const unsigned wi = atomicAdd(p.queue, 1u);
       cs.cell = wi < (unsigned)p.n_cells ? (p.order ? p.order[wi] : (int)wi) : -1;
     }
-    __syncthreads();
-    const int cell = cs.cell;
+    csync<CS>();
+    const int cell = *peer<CS>(&cs.cell, 0);
+    if constexpr (CS > 1) csync<CS>();  // rank 0's shared memory is read before any CTA may exit
     if (cell < 0) break;
     const int N = p.n_fine ? p.n_fine[cell] : p.n_fine_uniform;
     const int P = N + 3, n = N + 1, m = N - 1;
@@ -331,25 +378,28 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
 
     // ---------------- set-up ------------------------------------------
     if (tid < 8) { cs.iters[tid] = 0; cs.active[tid] = 1; cs.nu[tid] = 0.0; }
-    for (long i = tid; i < 22 * G; i += NT) c64[i] = 0.0;  // couplings, diagonal, phi~
+    for (long i = ctid; i < 22 * G; i += CNT) c64[i] = 0.0;  // couplings, diagonal, phi~
     const bool scalar = (p.coef_kind == MSFEM_COEF_TABULATED && p.ncomp == 1) ||
                         p.coef_kind == MSFEM_COEF_SINSIN;
     cell_geometry3d<NT>(p, cs, cell, N, scalar, tid);
     if (cs.status != MSFEM_CELL_CONVERGED) {
-      for (int i = tid; i < 64; i += NT) p.M[(int64_t)cell * 64 + i] = __longlong_as_double(0x7ff8000000000000ll);
-      if (tid < 8) {
-        p.F[(int64_t)cell * 8 + tid] = __longlong_as_double(0x7ff8000000000000ll);
-        if (p.iters) p.iters[(int64_t)cell * 8 + tid] = 0;
+      if (crank == 0) {
+        for (int i = tid; i < 64; i += NT) p.M[(int64_t)cell * 64 + i] = __longlong_as_double(0x7ff8000000000000ll);
+        if (tid < 8) {
+          p.F[(int64_t)cell * 8 + tid] = __longlong_as_double(0x7ff8000000000000ll);
+          if (p.iters) p.iters[(int64_t)cell * 8 + tid] = 0;
+        }
+        if (tid == 0) {
+          p.status[cell] = cs.status;
+          if (p.rel_res) p.rel_res[cell] = __longlong_as_double(0x7ff8000000000000ll);
+          if (p.refinements) p.refinements[cell] = 0;
+        }
       }
-      if (tid == 0) {
-        p.status[cell] = cs.status;
-        if (p.rel_res) p.rel_res[cell] = __longlong_as_double(0x7ff8000000000000ll);
-        if (p.refinements) p.refinements[cell] = 0;
-      }
-      __syncthreads();
+      csync<CS>();
       continue;
     }
 
+    csync<CS>();  // the workspace is zeroed by all CTAs of the cluster
     // ---------------- assembly: 8-colour scatter -------------------------
     {
       const int nfc = N * N * N;
@@ -360,7 +410,7 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
       for (int col = 0; col < 8; ++col) {
         const int ox = col & 1, oy = (col >> 1) & 1, oz = col >> 2;
         const int nx = (N - ox + 1) >> 1, ny = (N - oy + 1) >> 1, nz = (N - oz + 1) >> 1;
-        for (int idx = tid; idx < nx * ny * nz; idx += NT) {
+        for (int idx = ctid; idx < nx * ny * nz; idx += CNT) {
           const int cx = ox + 2 * (idx % nx), cy = oy + 2 * ((idx / nx) % ny), cz = oz + 2 * (idx / (nx * ny));
           double K[36];
           if (!element3d(p, cs, tab, N, cx, cy, cz, scalar, need_x, K)) cs.status = MSFEM_CELL_BAD_INPUT;
@@ -380,28 +430,31 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
             }
           }
         }
-        __syncthreads();
+        csync<CS>();
       }
     }
+    agree_status();
     if (cs.status != MSFEM_CELL_CONVERGED) {
-      for (int i = tid; i < 64; i += NT) p.M[(int64_t)cell * 64 + i] = __longlong_as_double(0x7ff8000000000000ll);
-      if (tid < 8) {
-        p.F[(int64_t)cell * 8 + tid] = __longlong_as_double(0x7ff8000000000000ll);
-        if (p.iters) p.iters[(int64_t)cell * 8 + tid] = 0;
+      if (crank == 0) {
+        for (int i = tid; i < 64; i += NT) p.M[(int64_t)cell * 64 + i] = __longlong_as_double(0x7ff8000000000000ll);
+        if (tid < 8) {
+          p.F[(int64_t)cell * 8 + tid] = __longlong_as_double(0x7ff8000000000000ll);
+          if (p.iters) p.iters[(int64_t)cell * 8 + tid] = 0;
+        }
+        if (tid == 0) {
+          p.status[cell] = cs.status;
+          if (p.rel_res) p.rel_res[cell] = __longlong_as_double(0x7ff8000000000000ll);
+          if (p.refinements) p.refinements[cell] = 0;
+        }
       }
-      if (tid == 0) {
-        p.status[cell] = cs.status;
-        if (p.rel_res) p.rel_res[cell] = __longlong_as_double(0x7ff8000000000000ll);
-        if (p.refinements) p.refinements[cell] = 0;
-      }
-      __syncthreads();
+      csync<CS>();
       continue;
     }
 
     // ---------------- symmetric scaling, Dirichlet data --------------------
     // D^-1/2 temporarily in r64[0]
     double dmin_part = 1e300;
-    for (int k = tid; k < nn; k += NT) {
+    for (int k = ctid; k < nn; k += CNT) {
       const int ix = k % n, iy = (k / n) % n, iz = k / (n * n);
       const int g = grid3(P, ix, iy, iz);
       const double d = d64[g];
@@ -412,12 +465,12 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
       }
     }
     // zero the ring entries of the temporary (read by the scaling below)
-    for (long i = tid; i < G; i += NT) {
+    for (long i = ctid; i < G; i += CNT) {
       const int ix = (int)(i % P) - 1, iy = (int)((i / P) % P) - 1, iz = (int)(i / ((long)P * P)) - 1;
       if (ix < 0 || iy < 0 || iz < 0 || ix > N || iy > N || iz > N) r64[i] = 0.0;
     }
-    __syncthreads();
-    for (int k = tid; k < nn; k += NT) {
+    csync<CS>();
+    for (int k = ctid; k < nn; k += CNT) {
       const int ix = k % n, iy = (k / n) % n, iz = k / (n * n);
       const int g = grid3(P, ix, iy, iz);
       const double s = r64[g];
@@ -427,8 +480,8 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
 #pragma unroll
     for (int mm = 16; mm >= 1; mm >>= 1) dmin_part = fmin(dmin_part, shfl_xor_d(dmin_part, mm));
     if (lane == 0) red[0][warp] = dmin_part;
-    __syncthreads();
-    for (int k = tid; k < nn; k += NT) {
+    csync<CS>();
+    for (int k = ctid; k < nn; k += CNT) {
       const int ix = k % n, iy = (k / n) % n, iz = k / (n * n);
       const int g = grid3(P, ix, iy, iz);
       if (ix == 0 || iy == 0 || iz == 0 || ix == N || iy == N || iz == N) {
@@ -443,10 +496,13 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
     }
     if (tid == 0) {
       double mn = 1e300;
-      for (int w = 0; w < NW; ++w) mn = fmin(mn, red[0][w]);
+      for (int c = 0; c < CS; ++c) {
+        const double *rc = peer<CS>(&red[0][0], c);
+        for (int w = 0; w < NW; ++w) mn = fmin(mn, rc[w]);
+      }
       cs.dmin = mn;
     }
-    __syncthreads();
+    csync<CS>();
 
     // interior node k -> grid index
     auto interior = [&](int k) {
@@ -459,7 +515,7 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
       double bbp[8];
 #pragma unroll
       for (int r = 0; r < 8; ++r) bbp[r] = 0.0;
-      for (int k = tid; k < nI; k += NT) {
+      for (int k = ctid; k < nI; k += CNT) {
         const int g = interior(k);
         double y[8];
         stencil27<double>(c64, x64, G, cs.offs, g, y);
@@ -472,10 +528,13 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
       }
       const double t = warp_transpose_reduce<8>(bbp, lane);
       if ((lane & 3) == 0) red[1][warp * 8 + (lane >> 2)] = t;
-      __syncthreads();
+      csync<CS>();
       if (warp == 0) {
         double s = 0.0;
-        for (int i = lane; i < NW * 8; i += 32) s += red[1][i];
+        for (int c = 0; c < CS; ++c) {
+            const double *rc = peer<CS>(&red[1][0], c);
+            for (int i = lane; i < NW * 8; i += 32) s += rc[i];
+          }
 #pragma unroll
         for (int mm = 8; mm < 32; mm <<= 1) s += shfl_xor_d(s, mm);
         if (lane < 8) cs.bb[lane] = s;
@@ -484,8 +543,8 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
     // warm start: x~0 = D^1/2 phi_warm, r = -(A~ phi~0)_I
     if (p.warm_basis != nullptr) {
       const double *wb = p.warm_basis + (p.basis_offset ? p.basis_offset[cell] : (int64_t)cell * 8 * nn);
-      __syncthreads();
-      for (int k = tid; k < nI; k += NT) {
+      csync<CS>();
+      for (int k = ctid; k < nI; k += CNT) {
         const int g = interior(k);
         const int ix = 1 + k % m, iy = 1 + (k / m) % m, iz = 1 + k / (m * m);
         const int node = (iz * n + iy) * n + ix;
@@ -493,8 +552,8 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
 #pragma unroll
         for (int r = 0; r < 8; ++r) x64[r * G + g] = __ldg(wb + (int64_t)r * nn + node) * sq;
       }
-      __syncthreads();
-      for (int k = tid; k < nI; k += NT) {
+      csync<CS>();
+      for (int k = ctid; k < nI; k += CNT) {
         const int g = interior(k);
         double y[8];
         stencil27<double>(c64, x64, G, cs.offs, g, y);
@@ -502,7 +561,7 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
         for (int r = 0; r < 8; ++r) r64[r * G + g] = -y[r];
       }
     }
-    __syncthreads();
+    csync<CS>();
     const double tol2 = p.tol * p.tol;
     int total_iters[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 
@@ -511,12 +570,12 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
     if (!MIXED) {
       // ================= plain FP64 CG (vectors in the workspace) ==========
       // p = r on the interior, 0 on boundary and ring
-      for (long i = tid; i < 8 * G; i += NT) p64[i] = 0.0;
-      __syncthreads();
+      for (long i = ctid; i < 8 * G; i += CNT) p64[i] = 0.0;
+      csync<CS>();
       double rp[16];
 #pragma unroll
       for (int r = 0; r < 16; ++r) rp[r] = 0.0;
-      for (int k = tid; k < nI; k += NT) {
+      for (int k = ctid; k < nI; k += CNT) {
         const int g = interior(k);
         const double d = d64[g];
 #pragma unroll
@@ -531,10 +590,13 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
         const double t = warp_transpose_reduce<16>(rp, lane);
         if ((lane & 1) == 0) red[0][warp * 16 + (lane >> 1)] = t;
       }
-      __syncthreads();
+      csync<CS>();
       if (warp == 0) {
         double s = 0.0;
-        for (int i = lane; i < NW * 16; i += 32) s += red[0][i];
+        for (int c = 0; c < CS; ++c) {
+            const double *rc = peer<CS>(&red[0][0], c);
+            for (int i = lane; i < NW * 16; i += 32) s += rc[i];
+          }
         s += shfl_xor_d(s, 16);
         const double nu = shfl_xor_d(s, 8);
         if (lane < 8) {
@@ -553,14 +615,14 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
           cs.need_nu = nn2 || p.check_interval == 1;
         }
       }
-      __syncthreads();
+      csync<CS>();
       int it = 0;
       while (!cs.done) {
         ++it;
         double sg[8];
 #pragma unroll
         for (int r = 0; r < 8; ++r) sg[r] = 0.0;
-        for (int k = tid; k < nI; k += NT) {
+        for (int k = ctid; k < nI; k += CNT) {
           const int g = interior(k);
           double y[8];
           stencil27<double>(c64, p64, G, cs.offs, g, y);
@@ -574,10 +636,13 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
           const double t = warp_transpose_reduce<8>(sg, lane);
           if ((lane & 3) == 0) red[1][warp * 8 + (lane >> 2)] = t;
         }
-        __syncthreads();
+        csync<CS>();
         if (warp == 0) {
           double s = 0.0;
-          for (int i = lane; i < NW * 8; i += 32) s += red[1][i];
+          for (int c = 0; c < CS; ++c) {
+            const double *rc = peer<CS>(&red[1][0], c);
+            for (int i = lane; i < NW * 8; i += 32) s += rc[i];
+          }
 #pragma unroll
           for (int mm = 8; mm < 32; mm <<= 1) s += shfl_xor_d(s, mm);
           if (lane < 8) {
@@ -598,14 +663,14 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
             cs.alpha[lane] = a;
           }
         }
-        __syncthreads();
+        csync<CS>();
         const bool need_nu = cs.need_nu;
         double al[8];
 #pragma unroll
         for (int r = 0; r < 8; ++r) al[r] = cs.alpha[r];
 #pragma unroll
         for (int r = 0; r < 16; ++r) rp[r] = 0.0;
-        for (int k = tid; k < nI; k += NT) {
+        for (int k = ctid; k < nI; k += CNT) {
           const int g = interior(k);
           const double d = d64[g];
 #pragma unroll
@@ -622,10 +687,13 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
           const double t = warp_transpose_reduce<16>(rp, lane);
           if ((lane & 1) == 0) red[0][warp * 16 + (lane >> 1)] = t;
         }
-        __syncthreads();
+        csync<CS>();
         if (warp == 0) {
           double s = 0.0;
-          for (int i = lane; i < NW * 16; i += 32) s += red[0][i];
+          for (int c = 0; c < CS; ++c) {
+            const double *rc = peer<CS>(&red[0][0], c);
+            for (int i = lane; i < NW * 16; i += 32) s += rc[i];
+          }
           s += shfl_xor_d(s, 16);
           const double nu = shfl_xor_d(s, 8);
           if (lane < 8) {
@@ -658,30 +726,30 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
             cs.need_nu = nn2 || (p.check_interval > 0 && ((it + 1) % p.check_interval) == 0);
           }
         }
-        __syncthreads();
+        csync<CS>();
         if (cs.done) break;
         double be[8];
 #pragma unroll
         for (int r = 0; r < 8; ++r) be[r] = cs.beta[r];
-        for (int k = tid; k < nI; k += NT) {
+        for (int k = ctid; k < nI; k += CNT) {
           const int g = interior(k);
 #pragma unroll
           for (int r = 0; r < 8; ++r) p64[r * G + g] = fma(be[r], p64[r * G + g], r64[r * G + g]);
         }
-        __syncthreads();
+        csync<CS>();
       }
     } else {
       // ================= MIXED: FP32 inner CG + FP64 refinement ===========
-      for (long i = tid; i < 13 * G; i += NT) c32[i] = (float)c64[i];
-      for (long i = tid; i < 8 * G; i += NT) pp32[i] = 0.0f;
-      __syncthreads();
+      for (long i = ctid; i < 13 * G; i += CNT) c32[i] = (float)c64[i];
+      for (long i = ctid; i < 8 * G; i += CNT) pp32[i] = 0.0f;
+      csync<CS>();
       const float itol2 = p.inner_tol * p.inner_tol;
       int ref = 0;
       for (;;) {
         double nup[8];
 #pragma unroll
         for (int r = 0; r < 8; ++r) nup[r] = 0.0;
-        for (int k = tid; k < nI; k += NT) {
+        for (int k = ctid; k < nI; k += CNT) {
           const int g = interior(k);
           const double d = d64[g];
 #pragma unroll
@@ -694,10 +762,13 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
           const double t = warp_transpose_reduce<8>(nup, lane);
           if ((lane & 3) == 0) red[0][warp * 8 + (lane >> 2)] = t;
         }
-        __syncthreads();
+        csync<CS>();
         if (warp == 0) {
           double s = 0.0;
-          for (int i = lane; i < NW * 8; i += 32) s += red[0][i];
+          for (int c = 0; c < CS; ++c) {
+            const double *rc = peer<CS>(&red[0][0], c);
+            for (int i = lane; i < NW * 8; i += 32) s += rc[i];
+          }
 #pragma unroll
           for (int mm = 8; mm < 32; mm <<= 1) s += shfl_xor_d(s, mm);
           if (lane < 8) {
@@ -721,7 +792,7 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
             cs.done = !any;
           }
         }
-        __syncthreads();
+        csync<CS>();
         if (cs.done) break;
         ++ref;
         float act[8];
@@ -730,7 +801,7 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
         float rho[8];
 #pragma unroll
         for (int r = 0; r < 8; ++r) rho[r] = 0.0f;
-        for (int k = tid; k < nI; k += NT) {
+        for (int k = ctid; k < nI; k += CNT) {
           const int g = interior(k);
 #pragma unroll
           for (int r = 0; r < 8; ++r) {
@@ -749,9 +820,12 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
           const float t = warp_transpose_reduce<8>(vv, lane);
           float *rb = reinterpret_cast<float *>(red[buf]);
           if ((lane & 3) == 0) rb[warp * 8 + (lane >> 2)] = t;
-          __syncthreads();
+          csync<CS>();
           float s = 0.f;
-          for (int i = lane; i < NW * 8; i += 32) s += rb[i];
+          for (int c = 0; c < CS; ++c) {
+            const float *rc = peer<CS>(rb, c);
+            for (int i = lane; i < NW * 8; i += 32) s += rc[i];
+          }
 #pragma unroll
           for (int mm = 8; mm < 32; mm <<= 1) s += shfl_xor_d(s, mm);
 #pragma unroll
@@ -779,7 +853,7 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
           float sg[8];
 #pragma unroll
           for (int r = 0; r < 8; ++r) sg[r] = 0.f;
-          for (int k = tid; k < nI; k += NT) {
+          for (int k = ctid; k < nI; k += CNT) {
             const int g = interior(k);
             float y[8];
             stencil27<float>(c32, pp32, G, cs.offs, g, y);
@@ -796,7 +870,7 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
             al[r] = (iact[r] && sg[r] > 0.f) ? rho[r] / sg[r] : 0.0f;
             rp[r] = 0.f;
           }
-          for (int k = tid; k < nI; k += NT) {
+          for (int k = ctid; k < nI; k += CNT) {
             const int g = interior(k);
 #pragma unroll
             for (int r = 0; r < 8; ++r) {
@@ -821,33 +895,34 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
               }
             }
           }
-          for (int k = tid; k < nI; k += NT) {
+          for (int k = ctid; k < nI; k += CNT) {
             const int g = interior(k);
 #pragma unroll
             for (int r = 0; r < 8; ++r) pp32[r * G + g] = fmaf(be[r], pp32[r * G + g], rr32[r * G + g]);
           }
-          __syncthreads();
+          csync<CS>();
         }
         // x~ += d (FP64); r = -(A~ phi~)_I in FP64
-        for (int k = tid; k < nI; k += NT) {
+        for (int k = ctid; k < nI; k += CNT) {
           const int g = interior(k);
 #pragma unroll
           for (int r = 0; r < 8; ++r) x64[r * G + g] += (double)dd32[r * G + g];
         }
-        __syncthreads();
-        for (int k = tid; k < nI; k += NT) {
+        csync<CS>();
+        for (int k = ctid; k < nI; k += CNT) {
           const int g = interior(k);
           double y[8];
           stencil27<double>(c64, x64, G, cs.offs, g, y);
 #pragma unroll
           for (int r = 0; r < 8; ++r) r64[r * G + g] = -y[r];
         }
-        __syncthreads();
+        csync<CS>();
       }
       if (tid == 0) cs.refinements = ref;
-      __syncthreads();
+      csync<CS>();
     }
 
+    agree_status();
     // ---------------- epilogue: M (64), F (8), true residual (8) -----------
     // x64 holds phi~ (the boundary values were never overwritten)
     const double fj = p.f_value;
@@ -855,7 +930,7 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
       double acc[32];
 #pragma unroll
       for (int i = 0; i < 32; ++i) acc[i] = 0.0;
-      for (int k = tid; k < nn; k += NT) {
+      for (int k = ctid; k < nn; k += CNT) {
         const int ix = k % n, iy = (k / n) % n, iz = k / (n * n);
         const int g = grid3(P, ix, iy, iz);
         if (part < 2) {
@@ -918,10 +993,13 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
       }
       const double tot = warp_transpose_reduce<32>(acc, lane);
       redE[warp * 32 + lane] = tot;
-      __syncthreads();
-      if (warp == 0) {
+      csync<CS>();
+      if (warp == 0 && crank == 0) {
         double s = 0.0;
-        for (int w = 0; w < NW; ++w) s += redE[w * 32 + lane];
+        for (int c = 0; c < CS; ++c) {
+          const double *rc = peer<CS>(&redE[0], c);
+          for (int w = 0; w < NW; ++w) s += rc[w * 32 + lane];
+        }
         if (part < 2) {
           p.M[(int64_t)cell * 64 + part * 32 + lane] = s;
         } else {
@@ -953,7 +1031,7 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
           }
         }
       }
-      __syncthreads();
+      csync<CS>();
     }
   }
 }
