@@ -699,7 +699,9 @@ namespace msfem {
 
 // Node features of N = 32 cells from the tabulated coefficient:
 // the tensor averaged over the node's fine cells (4 Gauss points each),
-// then (log a11, a12 / sqrt(a11 a22), log a22).
+// then (log a11, a12 / sqrt(a11 a22), log a22).  The inputs are FP64; the
+// arithmetic is FP32 (the features feed a BF16 network, and FP64 logarithms
+// at GB300's FP64 rate would cost more than the network itself).
 __global__ void features_kernel(const double *__restrict__ qp, int ncomp, const int64_t *__restrict__ qp_offset,
                                 int n_cells, float *__restrict__ feat) {
   constexpr int N = 32, n = 33, nfc = N * N;
@@ -708,7 +710,7 @@ __global__ void features_kernel(const double *__restrict__ qp, int ncomp, const 
   const double *tab = qp + (qp_offset ? qp_offset[cell] : (int64_t)cell * ncomp * 4 * nfc);
   for (int k = threadIdx.x; k < n * n; k += blockDim.x) {
     const int ix = k % n, iy = k / n;
-    double a[3] = {0.0, 0.0, 0.0};
+    float a[3] = {0.0f, 0.0f, 0.0f};
     int cnt = 0;
     for (int dy = -1; dy <= 0; ++dy)
       for (int dx = -1; dx <= 0; ++dx) {
@@ -718,20 +720,20 @@ __global__ void features_kernel(const double *__restrict__ qp, int ncomp, const 
         ++cnt;
         for (int q = 0; q < 4; ++q) {
           if (ncomp == 1) {
-            const double v = __ldg(tab + (int64_t)q * nfc + fc);
+            const float v = (float)__ldg(tab + (int64_t)q * nfc + fc);
             a[0] += v;
             a[2] += v;
           } else {
-            for (int c = 0; c < 3; ++c) a[c] += __ldg(tab + ((int64_t)c * 4 + q) * nfc + fc);
+            for (int c = 0; c < 3; ++c) a[c] += (float)__ldg(tab + ((int64_t)c * 4 + q) * nfc + fc);
           }
         }
       }
-    const double sc = 1.0 / (4.0 * cnt);
-    const double a11 = a[0] * sc, a12 = a[1] * sc, a22 = a[2] * sc;
+    const float sc = 1.0f / (4.0f * (float)cnt);
+    const float a11 = a[0] * sc, a12 = a[1] * sc, a22 = a[2] * sc;
     float *o = feat + (int64_t)cell * 3 * n * n + k;
-    o[0] = (float)log(a11);
-    o[n * n] = (float)(a12 / sqrt(a11 * a22));
-    o[2 * n * n] = (float)log(a22);
+    o[0] = logf(a11);
+    o[n * n] = a12 * rsqrtf(a11 * a22);
+    o[2 * n * n] = logf(a22);
   }
 }
 

@@ -111,3 +111,29 @@ def test_predict_is_independent_per_image(pkg, engine):
         sur.predict(feats[lo:hi].contiguous(), part)
         assert torch.equal(part, out[lo:hi])
     sur.close()
+
+
+@pytest.mark.gpu
+def test_features_match_numpy(pkg, engine):
+    """Network input (log a11, a12 / sqrt(a11 a22), log a22 of the tensor
+    averaged over each node's fine cells and Gauss points) against a numpy
+    restatement from the same tabulated coefficient; FP32 arithmetic on the
+    device, so 1e-5 relative to the feature scale."""
+    torch = pytest.importorskip("torch")
+    S, W = pkg.surrogate, pkg.workloads
+    prob = W.subset(W.config2(K=64, N=32), [0, 5, 2047, 4095])
+    desc, keep = S.device_problem(engine, prob, torch)
+    got = S.features(engine, desc, torch).cpu().numpy()
+    tab = engine.tabulate(prob, 3).reshape(4, 3, 4, 32, 32)  # [cell][comp][q][cy][cx]
+    cellavg = tab.mean(axis=2)                              # [cell][comp][cy][cx]
+    pad = np.zeros((4, 3, 34, 34))
+    cnt = np.zeros((34, 34))
+    pad[:, :, 1:33, 1:33] = cellavg
+    cnt[1:33, 1:33] = 1.0
+    # node (iy, ix) averages the fine cells (iy-1..iy, ix-1..ix) that exist
+    s = pad[:, :, :-1, :-1] + pad[:, :, 1:, :-1] + pad[:, :, :-1, 1:] + pad[:, :, 1:, 1:]
+    c = cnt[:-1, :-1] + cnt[1:, :-1] + cnt[:-1, 1:] + cnt[1:, 1:]
+    a = s / c
+    ref = np.stack([np.log(a[:, 0]), a[:, 1] / np.sqrt(a[:, 0] * a[:, 2]), np.log(a[:, 2])], axis=1)
+    assert got.shape == ref.shape
+    assert np.abs(got - ref).max() <= 1e-5 * max(1.0, np.abs(ref).max())
