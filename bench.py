@@ -59,6 +59,19 @@ def flops_per_solve_iter(N):
     return 2 * (3 * N - 5) ** 2 + 11 * (N - 1) ** 2
 
 
+def flops_per_solve_iter_3d(N):
+    """Algorithmic work of one CG iteration of one 3D solve: 2 nnz(A_II) +
+    11 n_I, nnz(A_II) = (3N-5)^3, n_I = (N-1)^3."""
+    return 2 * (3 * N - 5) ** 3 + 11 * (N - 1) ** 3
+
+
+def inner_flops_per_iter(N, poly):
+    """Inner FP32 iteration of the mixed 2D form with a polynomial
+    preconditioner of degree `poly` (poly + 1 stencils, two dot-product
+    pairs and the vector updates): (poly + 1) 2 nnz(A_II) + (11 + 4 poly) n_I."""
+    return (poly + 1) * 2 * (3 * N - 5) ** 2 + (11 + 4 * poly) * (N - 1) ** 2
+
+
 def flops_one_off_per_cell(N):
     """Epilogue 2^d 2 nnz + (2^2d + 2^d) 2 n^d, assembly N^d 2^d (2^2d (2d+1))."""
     n = N + 1
@@ -476,6 +489,11 @@ def main():
             "max_rel_residual": stmx["max_rel_residual"], "cells_failed": stmx["cells_failed"],
             "fp32_peak_tflops": fp32_peak.value / 1e12,
         }
+        # achieved FP32 work of the inner loop (algorithmic flops per inner
+        # iteration times the iterations executed) over the whole step time
+        fl32 = stmx["iterations_total"] * inner_flops_per_iter(N_FINE, int(tunemx.get("poly_degree", 0)))
+        line["mixed"]["inner_fp32_tflops"] = fl32 / (msmx * 1e-3) / 1e12
+        line["mixed"]["inner_fp32_frac_of_measured_peak"] = line["mixed"]["inner_fp32_tflops"] / (fp32_peak.value / 1e12)
     # ---- e2e through the public C-ABI with pinned host buffers
     if not args.no_e2e:
         tab_h = torch.empty(size, dtype=torch.float64, pin_memory=True)
@@ -610,6 +628,13 @@ def main():
                            "max_refinements": s4["refinements_max"],
                            "max_rel_residual": s4["max_rel_residual"], "cells_failed": s4["cells_failed"],
                            "tuning": tn.as_dict()}
+            # algorithmic CG work of the step (per solve: its iterations x the
+            # per-iteration flops of its N) against the FP64 / FP32 FMA peak
+            flw = float(sum(int(it_h[c].sum()) * flops_per_solve_iter_3d(int(nf4_h[c])) for c in range(nc4)))
+            peak = fp64_peak.value if prec == abi.PREC_FP64 else fp32_peak.value
+            res4[pname]["cg_tflops"] = flw / (ms * 1e-3) / 1e12
+            res4[pname]["cg_frac_of_measured_" + ("fp64" if prec == abi.PREC_FP64 else "fp32") + "_peak"] = \
+                flw / (ms * 1e-3) / peak
         res4["speedup_mixed_vs_fp64"] = res4["fp64"]["ms_per_step"] / res4["mixed"]["ms_per_step"]
         line["config4"] = res4
         del tab4, M4, F4, st4, it4, corners4, nf4

@@ -1,0 +1,78 @@
+"""Parity at the benchmark workloads' own sizes.
+
+Cells taken from the full config-3 field (256x256 coarse, N = 32) and from
+the full config-4 sphere field (112k spheres, N in {8, 16, 24}) against the
+oracle's direct solves (1e-10 relative, M and F); and, over whole batches,
+the size-independent properties of the coarse element matrices: symmetry,
+zero row sums (the basis is a partition of unity), positive
+semi-definiteness, and sum_cells sum_i F_i = integral of f over the domain."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_err(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def check_invariants(M, F, f_total, tol_rows, tol_f):
+    """tol_f: the basis solves stop at a 1e-10 relative residual, so
+    sum_i phi_i = 1 holds to the solve error, which grows with the condition
+    number (1e4-contrast spheres in 3D)."""
+    scale = np.abs(M).max(axis=(-2, -1))
+    asym = (np.abs(M - np.swapaxes(M, -1, -2)).max(axis=(-2, -1)) / scale).max()
+    rows = (np.abs(M.sum(axis=-1)).max(axis=-1) / scale).max()
+    lmin = (np.linalg.eigvalsh(M)[..., 0] / scale).min()
+    fsum = abs(F.sum() - f_total) / f_total
+    assert asym <= 1e-12, asym
+    assert rows <= tol_rows, rows
+    assert lmin >= -1e-10, lmin
+    assert fsum <= tol_f, fsum
+
+
+@pytest.fixture(scope="module")
+def config4_field(pkg):
+    return pkg.workloads.config4()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_config3_cells_against_oracle(pkg, oracle, engine, precision):
+    W = pkg.workloads
+    full = W.config3()
+    prob = W.subset(full, [0, 12345, 40000, 65535])
+    got = engine.run(prob, precision=precision, tol=1e-12)
+    ref = oracle.run(prob)
+    assert got["rc"] == 0 and np.all(got["status"] == 0)
+    assert rel_err(got["M"], ref["M"]) < 1e-10
+    assert rel_err(got["F"], ref["F"]) < 1e-10
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_config4_cells_against_oracle(pkg, oracle, engine, config4_field, precision):
+    W = pkg.workloads
+    nf = config4_field["n_fine_per_cell"]
+    cells = [int(np.flatnonzero(nf == v)[0]) for v in (24, 16, 8)] + [int(np.flatnonzero(nf == 24)[-1])]
+    prob = W.subset(config4_field, cells)
+    got = engine.run(prob, precision=precision, tol=1e-12)
+    ref = oracle.run(prob)
+    assert got["rc"] == 0 and np.all(got["status"] == 0)
+    assert rel_err(got["M"], ref["M"]) < 1e-9
+    assert rel_err(got["F"], ref["F"]) < 1e-10
+
+
+def test_config2_full_batch_invariants(pkg, engine):
+    prob = pkg.workloads.config2(K=64, N=32)
+    got = engine.run(prob, precision="fp64", tol=1e-10)
+    assert got["rc"] == 0 and np.all(got["status"] == 0)
+    check_invariants(got["M"], got["F"], 1.0, 1e-9, 1e-9)  # f = 1 on the unit square
+    mixed = engine.run(prob, precision="mixed", tol=1e-10)
+    assert mixed["rc"] == 0
+    assert rel_err(mixed["M"], got["M"]) < 1e-9
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_config4_full_batch_invariants(pkg, engine, config4_field, precision):
+    got = engine.run(config4_field, precision=precision, tol=1e-10)
+    assert got["rc"] == 0 and np.all(got["status"] == 0)
+    check_invariants(got["M"], got["F"], 1.0, 1e-9, 1e-6)  # f = 1 on the unit cube
