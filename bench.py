@@ -217,7 +217,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile", default=None, choices=["fp64_2d", "mixed_2d", "fp64_3d", "mixed_3d", "cnn"],
                     help="run one small single-kernel case (for ncu captures) and exit")
-    ap.add_argument("--variant", type=int, default=None, help="--profile 2D: launch shape index to use")
+    ap.add_argument("--variant", type=int, default=None, help="--profile: launch shape index to use")
     ap.add_argument("--inner-tol", type=float, default=1e-6, help="--profile 2D mixed: inner FP32 reduction")
     ap.add_argument("--cheb-ratio", type=float, default=30.0, help="--profile 2D mixed: Chebyshev interval ratio")
     ap.add_argument("--no-config3", action="store_true", help="skip the 65536-cell config-3 timing")
@@ -374,6 +374,9 @@ def main():
             # the first 256 cells of config 4 (uneven N, 1e4-contrast spheres)
             sub = W.subset(W.config4(), np.arange(256))
             prec = "fp64" if kind == "fp64_3d" else "mixed"
+            if args.variant is not None:
+                eng.set_tuning({"dim": 3, "n_max": 24, "precision": 0 if prec == "fp64" else 1,
+                                "variant": args.variant, "check_interval": 0, "inner_tol": args.inner_tol})
             for _ in range(args.warmup):
                 eng.run(sub, precision=prec, tol=TOL)
             t_ms = 0.0
