@@ -607,9 +607,12 @@ def main():
                 "cells_by_N": {str(v): int((nf4_h == v).sum()) for v in (8, 16, 24)},
                 "spheres": int(sp4.shape[0]), "sphere_generation_s": t_rsa}
         for prec, pname in ((abi.PREC_FP64, "fp64"), (abi.PREC_MIXED, "mixed")):
-            # autotune on the first 512 cells (the same N mix), then time the batch
+            # autotune on the first half of the batch (the same N mix; a
+            # sample large enough that every CTA works through several cells,
+            # as in the full batch), then time the batch
             tn = abi.Tuning()
-            rc = eng.lib.msfem_autotune(eng.handle, ctypes.byref(desc4(prec, 512)), 512, ctypes.byref(tn))
+            n_tune = nc4 // 2
+            rc = eng.lib.msfem_autotune(eng.handle, ctypes.byref(desc4(prec, n_tune)), n_tune, ctypes.byref(tn))
             if rc != abi.OK:
                 raise abi.MsfemError(rc, abi.last_error(eng.lib))
             d = desc4(prec)

@@ -701,13 +701,24 @@ namespace msfem {
 // the tensor averaged over the node's fine cells (4 Gauss points each),
 // then (log a11, a12 / sqrt(a11 a22), log a22).  The inputs are FP64; the
 // arithmetic is FP32 (the features feed a BF16 network, and FP64 logarithms
-// at GB300's FP64 rate would cost more than the network itself).
-__global__ void features_kernel(const double *__restrict__ qp, int ncomp, const int64_t *__restrict__ qp_offset,
-                                int n_cells, float *__restrict__ feat) {
+// at GB300's FP64 rate would cost more than the network itself).  Two
+// passes per cell: the Gauss-point sums of every fine cell (coalesced
+// reads of the component-major table, each value read once) into shared
+// memory, then the node averages.
+__global__ void __launch_bounds__(256) features_kernel(const double *__restrict__ qp, int ncomp,
+                                                       const int64_t *__restrict__ qp_offset, int n_cells,
+                                                       float *__restrict__ feat) {
   constexpr int N = 32, n = 33, nfc = N * N;
+  __shared__ float csum[3][nfc];
   const int cell = blockIdx.x;
   if (cell >= n_cells) return;
   const double *tab = qp + (qp_offset ? qp_offset[cell] : (int64_t)cell * ncomp * 4 * nfc);
+  for (int i = threadIdx.x; i < ncomp * nfc; i += blockDim.x) {
+    const int c = i / nfc, fc = i - c * nfc;
+    const double *t = tab + (int64_t)c * 4 * nfc + fc;
+    csum[c][fc] = (float)((__ldg(t) + __ldg(t + nfc)) + (__ldg(t + 2 * nfc) + __ldg(t + 3 * nfc)));
+  }
+  __syncthreads();
   for (int k = threadIdx.x; k < n * n; k += blockDim.x) {
     const int ix = k % n, iy = k / n;
     float a[3] = {0.0f, 0.0f, 0.0f};
@@ -718,18 +729,11 @@ __global__ void features_kernel(const double *__restrict__ qp, int ncomp, const 
         if (cx < 0 || cy < 0 || cx >= N || cy >= N) continue;
         const int fc = cx + N * cy;
         ++cnt;
-        for (int q = 0; q < 4; ++q) {
-          if (ncomp == 1) {
-            const float v = (float)__ldg(tab + (int64_t)q * nfc + fc);
-            a[0] += v;
-            a[2] += v;
-          } else {
-            for (int c = 0; c < 3; ++c) a[c] += (float)__ldg(tab + ((int64_t)c * 4 + q) * nfc + fc);
-          }
-        }
+        for (int c = 0; c < ncomp; ++c) a[c] += csum[c][fc];
       }
+    if (ncomp == 1) a[2] = a[0];
     const float sc = 1.0f / (4.0f * (float)cnt);
-    const float a11 = a[0] * sc, a12 = a[1] * sc, a22 = a[2] * sc;
+    const float a11 = a[0] * sc, a12 = ncomp == 1 ? 0.0f : a[1] * sc, a22 = a[2] * sc;
     float *o = feat + (int64_t)cell * 3 * n * n + k;
     o[0] = logf(a11);
     o[n * n] = a12 * rsqrtf(a11 * a22);

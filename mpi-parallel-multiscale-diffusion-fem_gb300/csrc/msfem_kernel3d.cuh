@@ -42,13 +42,15 @@ struct Work3D {
   static constexpr long kP64 = kR64 + 8 * G;   // [8][G] search direction (FP64 CG)
   static constexpr long kQ64 = kP64 + 8 * G;   // [8][G] A p
   static constexpr long kEnd64 = kQ64 + 8 * G;
-  // FP32 arrays (mixed form)
-  static constexpr long kC32 = 0;              // [13][G]
-  static constexpr long kD32 = kC32 + 13 * G;  // [8][G] correction d
-  static constexpr long kR32 = kD32 + 8 * G;   // [8][G]
-  static constexpr long kP32 = kR32 + 8 * G;   // [8][G]
-  static constexpr long kQ32 = kP32 + 8 * G;   // [8][G]
-  static constexpr long kEnd32 = kQ32 + 8 * G;
+  // FP32 arrays (mixed form): couplings [13][G], then the inner loop's
+  // node-major vectors [G][8] from a 16-byte boundary (G rounded up to G4)
+  static constexpr long G4 = (G + 3) & ~3L;
+  static constexpr long kC32 = 0;               // [13][G]
+  static constexpr long kD32 = kC32 + 13 * G4;  // [G][8] correction d
+  static constexpr long kR32 = kD32 + 8 * G4;   // [G][8] residual
+  static constexpr long kP32 = kR32 + 8 * G4;   // [G][8] search direction
+  static constexpr long kQ32 = kP32 + 8 * G4;   // [G][8] A p
+  static constexpr long kEnd32 = kQ32 + 8 * G4;
   // every slot starts on a 256-byte boundary (slot k at k * bytes())
   static constexpr size_t bytes(bool mixed) {
     return (sizeof(double) * kEnd64 + (mixed ? sizeof(float) * kEnd32 : 0) + 511) & ~size_t(255);
@@ -88,6 +90,7 @@ struct CellShared3D {
   double dmin;
   int active[8];
   int iters[8];
+  int inner_iters[8];  // mixed form: inner FP32 iterations per RHS
   int offs[13];        // grid offsets of the forward couplings
   int status;
   int affine;
@@ -213,6 +216,41 @@ __device__ __forceinline__ void stencil27(const T *__restrict__ c, const T *__re
     for (int r = 0; r < 8; ++r) {
       y[r] = fma(cf, v[r * G + g + d], y[r]);
       y[r] = fma(cb, v[r * G + g - d], y[r]);
+    }
+  }
+}
+
+// Node-major FP32 vectors ([node][8 RHS], 32-byte aligned nodes).
+__device__ __forceinline__ void ld8(const float *__restrict__ v, int g, float (&t)[8]) {
+  const float4 a = *reinterpret_cast<const float4 *>(v + 8 * (long)g);
+  const float4 b = *reinterpret_cast<const float4 *>(v + 8 * (long)g + 4);
+  t[0] = a.x; t[1] = a.y; t[2] = a.z; t[3] = a.w;
+  t[4] = b.x; t[5] = b.y; t[6] = b.z; t[7] = b.w;
+}
+__device__ __forceinline__ void st8(float *__restrict__ v, int g, const float (&t)[8]) {
+  *reinterpret_cast<float4 *>(v + 8 * (long)g) = make_float4(t[0], t[1], t[2], t[3]);
+  *reinterpret_cast<float4 *>(v + 8 * (long)g + 4) = make_float4(t[4], t[5], t[6], t[7]);
+}
+
+// y = A~ v at node g for 8 RHS, v node-major; vc = v at g.  The same
+// summation order as stencil27.
+__device__ __forceinline__ void stencil27_nm(const float *__restrict__ c, const float *__restrict__ v, long G,
+                                             const int *offs, int g, float (&y)[8], float (&vc)[8]) {
+  ld8(v, g, vc);
+#pragma unroll
+  for (int r = 0; r < 8; ++r) y[r] = vc[r];
+#pragma unroll
+  for (int o = 0; o < 13; ++o) {
+    const int d = offs[o];
+    const float cf = c[o * G + g];
+    const float cb = c[o * G + g - d];
+    float tf[8], tb[8];
+    ld8(v, g + d, tf);
+    ld8(v, g - d, tb);
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      y[r] = fmaf(cf, tf[r], y[r]);
+      y[r] = fmaf(cb, tb[r], y[r]);
     }
   }
 }
@@ -370,11 +408,13 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
     double *r64 = x64 + 8 * G;
     double *p64 = r64 + 8 * G;
     double *q64 = p64 + 8 * G;
+    // this cell's layout of the same slot (G <= Work3D::G, so G4 <= Work3D::G4)
+    const long G4 = (G + 3) & ~3L;
     float *c32 = W32;
-    float *dd32 = c32 + 13 * G;
-    float *rr32 = dd32 + 8 * G;
-    float *pp32 = rr32 + 8 * G;
-    float *qq32 = pp32 + 8 * G;
+    float *dd32 = c32 + 13 * G4;  // 16-byte aligned: node-major float4 accesses
+    float *rr32 = dd32 + 8 * G4;
+    float *pp32 = rr32 + 8 * G4;
+    float *qq32 = pp32 + 8 * G4;
 
     // ---------------- set-up ------------------------------------------
     if (tid < 8) { cs.iters[tid] = 0; cs.active[tid] = 1; cs.nu[tid] = 0.0; }
@@ -563,7 +603,7 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
     }
     csync<CS>();
     const double tol2 = p.tol * p.tol;
-    int total_iters[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (tid < 8) cs.inner_iters[tid] = 0;
 
     // 8-value block reduction finished by warp 0; returns after the barrier
     // with the totals in red[buf] lanes 0..7 read by every thread through cs
@@ -798,19 +838,26 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
         float act[8];
 #pragma unroll
         for (int r = 0; r < 8; ++r) act[r] = cs.active[r] ? 1.0f : 0.0f;
+        // The inner loop's FP32 vectors are node-major ([node][8 RHS], 32 B
+        // per node): a thread reads a neighbour's 8 values as two 16-byte
+        // loads, a warp reads 32 consecutive nodes as contiguous 1-KB runs,
+        // and the 13 offsets are unrolled so their loads are in flight
+        // together.
         float rho[8];
 #pragma unroll
         for (int r = 0; r < 8; ++r) rho[r] = 0.0f;
         for (int k = ctid; k < nI; k += CNT) {
           const int g = interior(k);
+          float rv[8];
 #pragma unroll
           for (int r = 0; r < 8; ++r) {
-            const float rv = (float)r64[r * G + g] * act[r];
-            rr32[r * G + g] = rv;
-            pp32[r * G + g] = rv;
-            dd32[r * G + g] = 0.0f;
-            rho[r] = fmaf(rv, rv, rho[r]);
+            rv[r] = (float)r64[r * G + g] * act[r];
+            rho[r] = fmaf(rv[r], rv[r], rho[r]);
           }
+          st8(rr32, g, rv);
+          st8(pp32, g, rv);
+          const float z[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+          st8(dd32, g, z);
         }
         int buf = 0;
         auto block_sum8 = [&](float (&v)[8]) {
@@ -833,80 +880,88 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
           buf ^= 1;
         };
         block_sum8(rho);
-        float rho0[8], itol2r[8];
-        bool iact[8];
+        // stopping threshold on r.r per RHS and the active set as a bit mask
+        // (few registers: the 2-CTA/SM shapes run at 64 per thread)
+        float thr[8];
+        unsigned iact = 0u;
 #pragma unroll
         for (int r = 0; r < 8; ++r) {
-          rho0[r] = rho[r];
-          iact[r] = act[r] > 0.0f && rho[r] > 0.0f;
+          if (act[r] > 0.0f && rho[r] > 0.0f) iact |= 1u << r;
           // never deeper than the outer goal needs (factor 10 margin)
           const double goal = cs.nu[r] > 0.0 ? 0.01 * tol2 * cs.bb[r] / cs.nu[r] : 0.0;
-          itol2r[r] = fmaxf(itol2, (float)fmin(goal, 0.25));
+          thr[r] = fmaxf(itol2, (float)fmin(goal, 0.25)) * rho[r];
         }
         int iit = 0;
         for (;;) {
-          bool any = false;
-#pragma unroll
-          for (int r = 0; r < 8; ++r) any |= iact[r];
-          if (!any || iit >= p.inner_maxit) break;
+          if (!iact || iit >= p.inner_maxit) break;
           ++iit;
           float sg[8];
 #pragma unroll
           for (int r = 0; r < 8; ++r) sg[r] = 0.f;
           for (int k = ctid; k < nI; k += CNT) {
             const int g = interior(k);
-            float y[8];
-            stencil27<float>(c32, pp32, G, cs.offs, g, y);
+            float y[8], pc[8];
+            stencil27_nm(c32, pp32, G, cs.offs, g, y, pc);
+            st8(qq32, g, y);
 #pragma unroll
-            for (int r = 0; r < 8; ++r) {
-              qq32[r * G + g] = y[r];
-              sg[r] = fmaf(pp32[r * G + g], y[r], sg[r]);
-            }
+            for (int r = 0; r < 8; ++r) sg[r] = fmaf(pc[r], y[r], sg[r]);
           }
           block_sum8(sg);
           float al[8], rp[8];
 #pragma unroll
           for (int r = 0; r < 8; ++r) {
-            al[r] = (iact[r] && sg[r] > 0.f) ? rho[r] / sg[r] : 0.0f;
+            al[r] = (((iact >> r) & 1u) && sg[r] > 0.f) ? rho[r] / sg[r] : 0.0f;
             rp[r] = 0.f;
           }
           for (int k = ctid; k < nI; k += CNT) {
             const int g = interior(k);
+            float dv[8], pv[8], qv[8], rv[8];
+            ld8(dd32, g, dv);
+            ld8(pp32, g, pv);
+            ld8(qq32, g, qv);
+            ld8(rr32, g, rv);
 #pragma unroll
             for (int r = 0; r < 8; ++r) {
-              dd32[r * G + g] = fmaf(al[r], pp32[r * G + g], dd32[r * G + g]);
-              const float rv = fmaf(-al[r], qq32[r * G + g], rr32[r * G + g]);
-              rr32[r * G + g] = rv;
-              rp[r] = fmaf(rv, rv, rp[r]);
+              dv[r] = fmaf(al[r], pv[r], dv[r]);
+              rv[r] = fmaf(-al[r], qv[r], rv[r]);
+              rp[r] = fmaf(rv[r], rv[r], rp[r]);
             }
+            st8(dd32, g, dv);
+            st8(rr32, g, rv);
           }
           block_sum8(rp);
           float be[8];
+          if (tid < 8 && ((iact >> tid) & 1u)) cs.inner_iters[tid] += 1;
 #pragma unroll
           for (int r = 0; r < 8; ++r) {
             be[r] = 0.0f;
-            if (iact[r]) {
-              total_iters[r] += 1;
-              if (!(rp[r] <= itol2r[r] * rho0[r]) && isfinite(rp[r])) {
+            if ((iact >> r) & 1u) {
+              if (!(rp[r] <= thr[r]) && isfinite(rp[r])) {
                 be[r] = rp[r] / rho[r];
                 rho[r] = rp[r];
               } else {
-                iact[r] = false;
+                iact &= ~(1u << r);
               }
             }
           }
           for (int k = ctid; k < nI; k += CNT) {
             const int g = interior(k);
+            float pv[8], rv[8];
+            ld8(pp32, g, pv);
+            ld8(rr32, g, rv);
 #pragma unroll
-            for (int r = 0; r < 8; ++r) pp32[r * G + g] = fmaf(be[r], pp32[r * G + g], rr32[r * G + g]);
+            for (int r = 0; r < 8; ++r) pv[r] = fmaf(be[r], pv[r], rv[r]);
+            st8(pp32, g, pv);
           }
           csync<CS>();
         }
         // x~ += d (FP64); r = -(A~ phi~)_I in FP64
         for (int k = ctid; k < nI; k += CNT) {
           const int g = interior(k);
+          float dv[8];
+          ld8(dd32, g, dv);
 #pragma unroll
-          for (int r = 0; r < 8; ++r) x64[r * G + g] += (double)dd32[r * G + g];
+          for (int r = 0; r < 8; ++r) x64[r * G + g] += (double)dv[r];
         }
         csync<CS>();
         for (int k = ctid; k < nI; k += CNT) {
@@ -935,7 +990,15 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
         const int g = grid3(P, ix, iy, iz);
         if (part < 2) {
           double y[8];
-          stencil27<double>(c64, x64, G, cs.offs, g, y);
+          const bool inner = ix > 0 && iy > 0 && iz > 0 && ix < N && iy < N && iz < N;
+          if (MIXED && inner) {
+            // interior rows: A~ phi~ = -r, the FP64 residual of the final
+            // iterate (computed after the last correction)
+#pragma unroll
+            for (int r = 0; r < 8; ++r) y[r] = -r64[r * G + g];
+          } else {
+            stencil27<double>(c64, x64, G, cs.offs, g, y);
+          }
 #pragma unroll
           for (int i = 0; i < 4; ++i) {
             const double ph = x64[(long)(4 * part + i) * G + g];
@@ -978,7 +1041,8 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
           const double s = rsqrt(d);
 #pragma unroll
           for (int i = 0; i < 8; ++i) acc[i] = fma(x64[(long)i * G + g], bl * s, acc[i]);
-          if (ix > 0 && iy > 0 && iz > 0 && ix < N && iy < N && iz < N) {
+          // true residual norm (the mixed form has it from its last check)
+          if (!MIXED && ix > 0 && iy > 0 && iz > 0 && ix < N && iy < N && iz < N) {
             double y[8];
             stencil27<double>(c64, x64, G, cs.offs, g, y);
 #pragma unroll
@@ -1015,7 +1079,7 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
           if (lane < 8 && p.iters) {
             const int itv = cs.iters[lane];
             p.iters[(int64_t)cell * 8 + lane] =
-                MIXED ? total_iters[lane] : (itv >= 0 ? itv : (itv <= -1000000 ? -itv - 1000000 : -itv));
+                MIXED ? cs.inner_iters[lane] : (itv >= 0 ? itv : (itv <= -1000000 ? -itv - 1000000 : -itv));
           }
           if (lane == 0) {
             int st = cs.status;
