@@ -91,6 +91,8 @@ struct CellShared3D {
   int active[8];
   int iters[8];
   int inner_iters[8];  // mixed form: inner FP32 iterations per RHS
+  float seg_thr[8];    // mixed form: stopping threshold on r.r of the current segment
+  float seg_rho[2][8]; // mixed form: r.r of the current and next inner iteration
   int offs[13];        // grid offsets of the forward couplings
   int status;
   int affine;
@@ -355,6 +357,118 @@ template <int CS, typename T>
 __device__ __forceinline__ T *peer(T *ptr, int rank) {
   if constexpr (CS > 1) return cooperative_groups::this_cluster().map_shared_rank(ptr, rank);
   else return ptr;
+}
+
+// One refinement segment of the mixed form's inner FP32 CG (at most
+// inner_maxit iterations, per-RHS stopping at r.r <= thr) on the node-major
+// FP32 vectors.  Kept out of line: the kernel's FP64-phase state is saved
+// once per segment rather than held in registers through the FP32 loop (the
+// 2-CTA/SM shapes run at 64 registers per thread).  Reductions use red[buf],
+// red[buf ^ 1] alternately, buf as left by the caller's last reduction.
+template <int NT, int CS>
+__device__ __noinline__ void inner_segment3d(const float *__restrict__ c32, float *pp32, float *qq32,
+                                             float *rr32, float *dd32, long G, int m, int P, int nI,
+                                             int inner_maxit, unsigned iact, int buf,
+                                             double (*red)[NT / 32 * 16], CellShared3D &cs) {
+  constexpr int NW = NT / 32;
+  constexpr int CNT = NT * CS;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int ctid = cluster_rank<CS>() * NT + tid;
+  auto interior = [&](int k) {
+    const int ix = 1 + k % m, iy = 1 + (k / m) % m, iz = 1 + k / (m * m);
+    return grid3(P, ix, iy, iz);
+  };
+  auto block_sum8 = [&](float (&v)[8]) {
+    float vv[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) vv[r] = v[r];
+    const float t = warp_transpose_reduce<8>(vv, lane);
+    float *rb = reinterpret_cast<float *>(red[buf]);
+    if ((lane & 3) == 0) rb[warp * 8 + (lane >> 2)] = t;
+    csync<CS>();
+    float s = 0.f;
+    for (int c = 0; c < CS; ++c) {
+      const float *rc = peer<CS>(rb, c);
+      for (int i = lane; i < NW * 8; i += 32) s += rc[i];
+    }
+#pragma unroll
+    for (int mm = 8; mm < 32; mm <<= 1) s += shfl_xor_d(s, mm);
+#pragma unroll
+    for (int r = 0; r < 8; ++r) v[r] = __shfl_sync(0xffffffffu, s, r);
+    buf ^= 1;
+  };
+  // r.r per RHS in shared memory (seg_rho[par], double-buffered so that
+  // every thread reads the old values while the next ones are written) and
+  // the stopping thresholds seg_thr: 16 registers fewer in the node loops
+  int par = 0;
+  int iit = 0;
+  for (;;) {
+    if (!iact || iit >= inner_maxit) break;
+    ++iit;
+    float sg[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) sg[r] = 0.f;
+    for (int k = ctid; k < nI; k += CNT) {
+      const int g = interior(k);
+      float y[8], pc[8];
+      stencil27_nm(c32, pp32, G, cs.offs, g, y, pc);
+      st8(qq32, g, y);
+#pragma unroll
+      for (int r = 0; r < 8; ++r) sg[r] = fmaf(pc[r], y[r], sg[r]);
+    }
+    block_sum8(sg);
+    float al[8], rp[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      al[r] = (((iact >> r) & 1u) && sg[r] > 0.f) ? cs.seg_rho[par][r] / sg[r] : 0.0f;
+      rp[r] = 0.f;
+    }
+    for (int k = ctid; k < nI; k += CNT) {
+      const int g = interior(k);
+      float dv[8], pv[8], qv[8], rv[8];
+      ld8(dd32, g, dv);
+      ld8(pp32, g, pv);
+      ld8(qq32, g, qv);
+      ld8(rr32, g, rv);
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        dv[r] = fmaf(al[r], pv[r], dv[r]);
+        rv[r] = fmaf(-al[r], qv[r], rv[r]);
+        rp[r] = fmaf(rv[r], rv[r], rp[r]);
+      }
+      st8(dd32, g, dv);
+      st8(rr32, g, rv);
+    }
+    block_sum8(rp);
+    float be[8];
+    if (tid < 8 && ((iact >> tid) & 1u)) cs.inner_iters[tid] += 1;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      be[r] = 0.0f;
+      const float rho = cs.seg_rho[par][r];
+      float next = rho;
+      if ((iact >> r) & 1u) {
+        if (!(rp[r] <= cs.seg_thr[r]) && isfinite(rp[r])) {
+          be[r] = rp[r] / rho;
+          next = rp[r];
+        } else {
+          iact &= ~(1u << r);
+        }
+      }
+      if (tid == r) cs.seg_rho[par ^ 1][r] = next;
+    }
+    par ^= 1;
+    for (int k = ctid; k < nI; k += CNT) {
+      const int g = interior(k);
+      float pv[8], rv[8];
+      ld8(pp32, g, pv);
+      ld8(rr32, g, rv);
+#pragma unroll
+      for (int r = 0; r < 8; ++r) pv[r] = fmaf(be[r], pv[r], rv[r]);
+      st8(pp32, g, pv);
+    }
+    csync<CS>();
+  }
 }
 
 template <int NT, bool MIXED, int MINB, int CS>
@@ -891,70 +1005,18 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
           const double goal = cs.nu[r] > 0.0 ? 0.01 * tol2 * cs.bb[r] / cs.nu[r] : 0.0;
           thr[r] = fmaxf(itol2, (float)fmin(goal, 0.25)) * rho[r];
         }
-        int iit = 0;
-        for (;;) {
-          if (!iact || iit >= p.inner_maxit) break;
-          ++iit;
-          float sg[8];
-#pragma unroll
-          for (int r = 0; r < 8; ++r) sg[r] = 0.f;
-          for (int k = ctid; k < nI; k += CNT) {
-            const int g = interior(k);
-            float y[8], pc[8];
-            stencil27_nm(c32, pp32, G, cs.offs, g, y, pc);
-            st8(qq32, g, y);
-#pragma unroll
-            for (int r = 0; r < 8; ++r) sg[r] = fmaf(pc[r], y[r], sg[r]);
-          }
-          block_sum8(sg);
-          float al[8], rp[8];
+        if (tid < 8) {
+          float t = 0.f, q = 0.f;
 #pragma unroll
           for (int r = 0; r < 8; ++r) {
-            al[r] = (((iact >> r) & 1u) && sg[r] > 0.f) ? rho[r] / sg[r] : 0.0f;
-            rp[r] = 0.f;
+            t = r == tid ? thr[r] : t;
+            q = r == tid ? rho[r] : q;
           }
-          for (int k = ctid; k < nI; k += CNT) {
-            const int g = interior(k);
-            float dv[8], pv[8], qv[8], rv[8];
-            ld8(dd32, g, dv);
-            ld8(pp32, g, pv);
-            ld8(qq32, g, qv);
-            ld8(rr32, g, rv);
-#pragma unroll
-            for (int r = 0; r < 8; ++r) {
-              dv[r] = fmaf(al[r], pv[r], dv[r]);
-              rv[r] = fmaf(-al[r], qv[r], rv[r]);
-              rp[r] = fmaf(rv[r], rv[r], rp[r]);
-            }
-            st8(dd32, g, dv);
-            st8(rr32, g, rv);
-          }
-          block_sum8(rp);
-          float be[8];
-          if (tid < 8 && ((iact >> tid) & 1u)) cs.inner_iters[tid] += 1;
-#pragma unroll
-          for (int r = 0; r < 8; ++r) {
-            be[r] = 0.0f;
-            if ((iact >> r) & 1u) {
-              if (!(rp[r] <= thr[r]) && isfinite(rp[r])) {
-                be[r] = rp[r] / rho[r];
-                rho[r] = rp[r];
-              } else {
-                iact &= ~(1u << r);
-              }
-            }
-          }
-          for (int k = ctid; k < nI; k += CNT) {
-            const int g = interior(k);
-            float pv[8], rv[8];
-            ld8(pp32, g, pv);
-            ld8(rr32, g, rv);
-#pragma unroll
-            for (int r = 0; r < 8; ++r) pv[r] = fmaf(be[r], pv[r], rv[r]);
-            st8(pp32, g, pv);
-          }
-          csync<CS>();
+          cs.seg_thr[tid] = t;
+          cs.seg_rho[0][tid] = q;
         }
+        __syncthreads();
+        inner_segment3d<NT, CS>(c32, pp32, qq32, rr32, dd32, G, m, P, nI, p.inner_maxit, iact, buf, red, cs);
         // x~ += d (FP64); r = -(A~ phi~)_I in FP64
         for (int k = ctid; k < nI; k += CNT) {
           const int g = interior(k);
