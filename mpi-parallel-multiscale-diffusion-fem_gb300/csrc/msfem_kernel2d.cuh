@@ -111,6 +111,7 @@ struct CellShared2D {
   int iters[4];
   int status;
   int affine;
+  int axis;           // affine cell with axis-aligned edges: G = diag(jinv_g[0], jinv_g[4], jinv_g[8]) A
   int need_nu;
   int done;
   int cell;
@@ -159,6 +160,7 @@ __device__ int cell_geometry2d(const KernelParams &p, CellShared2D &cs, int cell
     // parallelogram test v0 + v3 == v1 + v2 (exact)
     const int aff = (cr[0] + cr[6] == cr[2] + cr[4]) && (cr[1] + cr[7] == cr[3] + cr[5]);
     cs.affine = aff;
+    cs.axis = aff && cr[3] == cr[1] && cr[4] == cr[0];
     cs.refinements = 0;
     if (aff && st == MSFEM_CELL_CONVERGED) {
       const double invN = 1.0 / (double)N;
@@ -229,9 +231,16 @@ __device__ __forceinline__ bool element2d(const KernelParams &p, const CellShare
         xq[1] = cs.corners[1] + cs.jfine[1] * u + cs.jfine[3] * v;
       }
       coef_at<2>(p, xq, tab, q, nfc, fc, A);
-      G11[q] = cs.jinv_g[0] * A[0] + cs.jinv_g[1] * A[1] + cs.jinv_g[2] * A[2];
-      G12[q] = cs.jinv_g[3] * A[0] + cs.jinv_g[4] * A[1] + cs.jinv_g[5] * A[2];
-      G22[q] = cs.jinv_g[6] * A[0] + cs.jinv_g[7] * A[1] + cs.jinv_g[8] * A[2];
+      if (cs.axis) {
+        // the other six entries of jinv_g are zero: the same sums, 3 products
+        G11[q] = cs.jinv_g[0] * A[0];
+        G12[q] = cs.jinv_g[4] * A[1];
+        G22[q] = cs.jinv_g[8] * A[2];
+      } else {
+        G11[q] = cs.jinv_g[0] * A[0] + cs.jinv_g[1] * A[1] + cs.jinv_g[2] * A[2];
+        G12[q] = cs.jinv_g[3] * A[0] + cs.jinv_g[4] * A[1] + cs.jinv_g[5] * A[2];
+        G22[q] = cs.jinv_g[6] * A[0] + cs.jinv_g[7] * A[1] + cs.jinv_g[8] * A[2];
+      }
     }
     const double Ay[2] = {G11[0] + G11[1], G11[2] + G11[3]};  // sum over qx
     const double Bx[2] = {G22[0] + G22[2], G22[1] + G22[3]};  // sum over qy
@@ -1004,14 +1013,17 @@ msfem2d_mixed_kernel(const KernelParams p) {
     const int ns = own ? min(S, N - s0) : 0;
     const int g0 = (s0 + 1) * P + ix + 1;
 
-    // FP64 right-hand sides (and warm start)
+    // FP64 right-hand sides b~ = -(A~ phi~)_I (and warm start).  phi~ is
+    // zero inside, so b~ vanishes at every node not next to the boundary:
+    // the stencil runs on the boundary-adjacent rows and columns only.
     double r64[S][4];
     double bbp[4] = {0.0, 0.0, 0.0, 0.0};
+    const bool edge_col = ix == 1 || ix == N - 1;
 #pragma unroll
     for (int s = 0; s < S; ++s) {
 #pragma unroll
       for (int r = 0; r < 4; ++r) r64[s][r] = 0.0;
-      if (s < ns) {
+      if (s < ns && (edge_col || s0 + s == 1 || s0 + s == N - 1)) {
         double y[4];
         stencil9<double>(c64, v64, g0 + s * P, P, y);
         const double d = d64[g0 + s * P];
