@@ -529,6 +529,26 @@ def main():
                        "d2h_bytes_per_step": int(M_h.numel() * 8 + F_h.numel() * 8 + st_h.numel() * 4)}
         # sanity: host result equals the device-resident one
         line["e2e"]["matches_device"] = bool(np.array_equal(M_h.numpy(), M64))
+        line["e2e"]["note"] = ("pinned host table read in place by the kernel over the CPU-GPU link "
+                               "(counted in h2d_bytes_per_step); M/F/status copied back")
+        # the mixed form through the same host call
+        if not args.no_mixed:
+            dm = device_desc(ws2, abi.PREC_MIXED)
+            dm.memory = abi.MEM_HOST
+            dm.corners = corners_pin.data_ptr()
+            dm.coef.qp_values = tab_h.data_ptr()
+            for _ in range(2):
+                eng.run_desc(dm, M_h.data_ptr(), F_h.data_ptr(), None, st_h.data_ptr(), None, stats=False)
+            torch.cuda.synchronize()
+            barrier()
+            t0 = time.perf_counter()
+            for _ in range(e_steps):
+                eng.run_desc(dm, M_h.data_ptr(), F_h.data_ptr(), None, st_h.data_ptr(), None, stats=False)
+            torch.cuda.synchronize()
+            e2e_m = max_over_ranks((time.perf_counter() - t0) / e_steps)
+            line["mixed"]["e2e"] = {"value": world * solves_rank / e2e_m, "unit": UNIT, "ms_per_step": e2e_m * 1e3,
+                                    "h2d_bytes_per_step": line["e2e"]["h2d_bytes_per_step"],
+                                    "d2h_bytes_per_step": line["e2e"]["d2h_bytes_per_step"]}
     # ---- config 3 workload: 256x256 coarse cells (65536), mixed vs FP64
     if not args.no_config3 and world == 1 and args.coarse == K_COARSE:
         ws3 = make_ws(W.config3(), 0)

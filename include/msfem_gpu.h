@@ -116,7 +116,9 @@ typedef enum msfem_precision {
 } msfem_precision;
 
 typedef enum msfem_memory {
-  MSFEM_MEM_HOST = 0,           /* all descriptor/output pointers are host memory */
+  MSFEM_MEM_HOST = 0,           /* all descriptor/output pointers are host memory; inputs of
+                                   1 MB or more in pinned (device-mapped) memory are read in
+                                   place by the kernels, pageable ones are copied */
   MSFEM_MEM_DEVICE = 1          /* all descriptor/output pointers are device memory */
 } msfem_memory;
 

@@ -277,6 +277,22 @@ int upload(msfem_handle *h, DevBuf &buf, const T *src, size_t count, bool device
     *dst = src;
     return MSFEM_OK;
   }
+  // Large inputs in pinned (page-locked, device-mapped) host memory are read
+  // in place by the kernels over the CPU-GPU link (NVLink-C2C on Grace
+  // nodes): each value is read once, spread over the whole launch, instead
+  // of a copy that must finish before the launch starts.  The caller's buffer
+  // is only read while the call runs (host-memory calls synchronise before
+  // returning).  Pageable memory is copied.
+  if (count * sizeof(T) >= (size_t(1) << 20)) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, src) == cudaSuccess && a.type == cudaMemoryTypeHost &&
+        a.devicePointer != nullptr) {
+      *dst = static_cast<const T *>(a.devicePointer);
+      *h2d += (int64_t)(count * sizeof(T));
+      return MSFEM_OK;
+    }
+    (void)cudaGetLastError();
+  }
   MSFEM_CUDA(buf.ensure(count * sizeof(T)));
   MSFEM_CUDA(cudaMemcpyAsync(buf.ptr, src, count * sizeof(T), cudaMemcpyHostToDevice, h->stream));
   *h2d += (int64_t)(count * sizeof(T));
