@@ -10,11 +10,12 @@
 //
 // A 3D local problem with 8 right-hand sides does not fit one SM's shared
 // memory (N = 24: 15625 nodes x 176 B in FP64), so each persistent CTA owns
-// a slot of a global-memory workspace with structure-of-arrays vectors
-// ([component][node], coalesced along x).  The working set of one sweep
-// (three node planes) stays in L1; the couplings stream from L2.  Bound: the
-// FP64 pipe in the FP64 form (26 FMA x 8 RHS per node per iteration against
-// ~100 B of couplings), L1/L2 bandwidth in the FP32 inner loop.
+// a slot of a global-memory workspace: FP64 arrays structure-of-arrays
+// ([component][node], coalesced along x), the mixed form's inner FP32 CG
+// vectors node-major ([node][8 RHS], two 16-byte loads per neighbour).  The
+// working set of one sweep (three node planes) stays in L1.  Bound: the FP64
+// pipe in the FP64 form (26 FMA x 8 RHS per node per iteration against
+// ~100 B of couplings), L1 throughput in the FP32 inner loop.
 //
 // Node (ix,iy,iz) of the (N+1)^3 grid sits at g = ((iz+1) P + iy + 1) P + ix + 1,
 // P = N + 3 (a zero ring around the grid).  Each node stores its 13 "forward"
