@@ -133,7 +133,8 @@ typedef struct msfem_coef_desc {
   int32_t ncomp;                /* TABULATED only */
   double params[8];
   const double *qp_values;      /* TABULATED */
-  const int64_t *qp_offset;     /* TABULATED, per-cell offset in doubles; NULL = uniform blocks */
+  const int64_t *qp_offset;     /* TABULATED, per-cell offset in doubles; NULL = packed cell
+                                   blocks of ncomp 2^d N_c^d doubles in cell order */
   const double *modes;          /* FOURIER [n_fields][n_modes][5] */
   int32_t n_modes;
   int32_t n_spheres;
@@ -216,6 +217,23 @@ int msfem_run_batch(msfem_handle *handle, const msfem_batch_desc *desc,
 int msfem_energy_error(msfem_handle *handle, const msfem_batch_desc *desc,
                        const double *basis, const double *basis_ref,
                        double *err, double *ref_norm);
+
+/* Fine-scale solution in every cell from its multiscale basis and the
+ * coarse solution: u[cell][node] = sum_i w[cell][i] phi_i[cell][node].
+ * Replaces set_global_weights + the per-cell reconstruction of the fine
+ * solution (diffusion_problem_basis.tpp:352-377, used by
+ * diffusion_problem_ms.tpp:299-325 for output).
+ *   basis    msfem_run_batch's basis layout ([cell][2^d][(N+1)^d]; uneven N:
+ *            cell blocks of 2^d (N_c+1)^d)
+ *   weights  [n_cells][2^d], the coarse solution at the cell's vertices in
+ *            the order of M/F
+ *   u        [cell][(N+1)^d] lexicographic fine nodes (uneven N: cell blocks
+ *            of (N_c+1)^d)
+ * desc supplies dim, n_cells, N (uniform or per cell) and the memory mode;
+ * its coefficient is not used.  DEVICE calls are asynchronous on the
+ * handle's stream. */
+int msfem_reconstruct(msfem_handle *handle, const msfem_batch_desc *desc, const double *basis,
+                      const double *weights, double *u);
 
 /* Evaluate the coefficient of desc->coef (any analytic kind) at the Gauss
  * points of every fine cell of the batch, in the TABULATED layout, on the

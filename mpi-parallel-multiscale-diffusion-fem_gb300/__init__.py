@@ -4,8 +4,9 @@ include/base/diffusion_problem_basis.tpp:438-474).
 
 The product is the CUDA library lib/libmsfem_gpu.so behind the C-ABI
 include/msfem_gpu.h; this package builds it (build.py), binds it (_abi.py,
-engine.py) and describes workloads (workloads.py).  It is imported under the
+engine.py), describes workloads (workloads.py) and stores tabulated
+coefficient fields on disk (fieldio.py).  It is imported under the
 name ``msfem_gb300`` (the folder name is not an identifier).
 """
-from . import _abi, build, engine, sharding, surrogate, workloads  # noqa: F401
+from . import _abi, build, engine, fieldio, sharding, surrogate, workloads  # noqa: F401
 from .engine import Engine  # noqa: F401

@@ -139,6 +139,8 @@ EXPORTS = {
     "msfem_energy_error": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BatchDesc),
                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.c_void_p]),
+    "msfem_reconstruct": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BatchDesc), ctypes.c_void_p,
+                                         ctypes.c_void_p, ctypes.c_void_p]),
     "msfem_tabulate_coefficient": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BatchDesc),
                                                   ctypes.c_int32, ctypes.c_void_p]),
     "msfem_tabulated_size": (ctypes.c_int64, [ctypes.POINTER(BatchDesc), ctypes.c_int32]),

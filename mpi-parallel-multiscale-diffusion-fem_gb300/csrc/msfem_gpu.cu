@@ -757,6 +757,32 @@ __global__ void __launch_bounds__(256) features_kernel(const double *__restrict_
   }
 }
 
+// Fine-scale solution of every cell, u = sum_i w_i phi_i over its nodes
+// (set_global_weights and the per-cell reconstruction of
+// diffusion_problem_basis.tpp:352-377).  One CTA per cell (grid-stride over
+// cells), coalesced along the nodes; HBM-bound: 2^d + 1 doubles per node.
+__global__ void reconstruct_kernel(int dim, int n_cells, int n_uniform, const int32_t *__restrict__ n_fine,
+                                   const int64_t *__restrict__ boff, const double *__restrict__ basis,
+                                   const double *__restrict__ w, double *__restrict__ u) {
+  const int nv = 1 << dim;
+  for (int cell = blockIdx.x; cell < n_cells; cell += gridDim.x) {
+    const int n = (n_fine ? n_fine[cell] : n_uniform) + 1;
+    const int nn = dim == 2 ? n * n : n * n * n;
+    const int64_t b0 = boff ? boff[cell] : (int64_t)cell * nv * nn;
+    const int64_t u0 = b0 / nv;
+    double wc[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) wc[i] = i < nv ? __ldg(w + (int64_t)cell * nv + i) : 0.0;
+    for (int k = threadIdx.x; k < nn; k += blockDim.x) {
+      double s = 0.0;
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+        if (i < nv) s = fma(wc[i], __ldg(basis + b0 + (int64_t)i * nn + k), s);
+      u[u0 + k] = s;
+    }
+  }
+}
+
 // Warm basis = Q1 hat + predicted correction, FP64 [cell][4][33*33].
 __global__ void compose_warm_kernel(const float *__restrict__ delta, int n_cells, double *__restrict__ warm) {
   constexpr int n = 33, nn = n * n;
@@ -1528,6 +1554,51 @@ int msfem_energy_error(msfem_handle *h, const msfem_batch_desc *d, const double 
   if (!dev) {
     MSFEM_CUDA(cudaMemcpyAsync(err, e, sizeof(double) * nc * nv, cudaMemcpyDeviceToHost, h->stream));
     MSFEM_CUDA(cudaMemcpyAsync(ref_norm, n, sizeof(double) * nc * nv, cudaMemcpyDeviceToHost, h->stream));
+    MSFEM_CUDA(cudaStreamSynchronize(h->stream));
+  }
+  return MSFEM_OK;
+}
+
+int msfem_reconstruct(msfem_handle *h, const msfem_batch_desc *d, const double *basis, const double *weights,
+                      double *u) {
+  if (!h) return fail(MSFEM_ERR_INVALID_ARG, "handle is NULL");
+  int rc = validate(d);
+  if (rc) return rc;
+  if (d->n_cells > 0 && (!basis || !weights || !u))
+    return fail(MSFEM_ERR_INVALID_ARG, "basis, weights and u are required");
+  if (d->n_cells == 0) return MSFEM_OK;
+  MSFEM_CUDA(cudaSetDevice(h->device));
+  const int dim = d->dim, nv = 1 << dim, nc = d->n_cells;
+  const bool dev = d->memory == MSFEM_MEM_DEVICE;
+  std::vector<int32_t> nf;
+  if ((rc = host_nfine(h, d, nf))) return rc;
+  int64_t h2d = 0, basis_total = (int64_t)nc * nv * ipow(d->n_fine + 1, dim);
+  const int32_t *nfd = nullptr;
+  const int64_t *boffd = nullptr;
+  if (d->n_fine_per_cell) {
+    std::vector<int64_t> boff(nc);
+    basis_total = 0;
+    for (int c = 0; c < nc; ++c) {
+      boff[c] = basis_total;
+      basis_total += (int64_t)nv * ipow(nf[c] + 1, dim);
+    }
+    if ((rc = upload<int32_t>(h, h->nfine, d->n_fine_per_cell, (size_t)nc, dev, &nfd, &h2d))) return rc;
+    if ((rc = upload<int64_t>(h, h->boff, boff.data(), boff.size(), false, &boffd, &h2d))) return rc;
+  }
+  const double *b = nullptr, *w = nullptr;
+  if ((rc = upload<double>(h, h->basis, basis, (size_t)basis_total, dev, &b, &h2d))) return rc;
+  if ((rc = upload<double>(h, h->F, weights, (size_t)nc * nv, dev, &w, &h2d))) return rc;
+  const int64_t u_total = basis_total / nv;
+  double *ud = u;
+  if (!dev) {
+    MSFEM_CUDA(h->warm.ensure(sizeof(double) * (size_t)u_total));
+    ud = h->warm.as<double>();
+  }
+  const int grid = std::max(1, std::min(nc, 8 * h->sm_count));
+  msfem::reconstruct_kernel<<<grid, 256, 0, h->stream>>>(dim, nc, d->n_fine, nfd, boffd, b, w, ud);
+  MSFEM_CUDA(cudaGetLastError());
+  if (!dev) {
+    MSFEM_CUDA(cudaMemcpyAsync(u, ud, sizeof(double) * (size_t)u_total, cudaMemcpyDeviceToHost, h->stream));
     MSFEM_CUDA(cudaStreamSynchronize(h->stream));
   }
   return MSFEM_OK;

@@ -154,6 +154,21 @@ class Engine:
             raise _abi.MsfemError(rc, _abi.last_error(self.lib))
         return err, nrm
 
+    def reconstruct(self, problem, basis, weights):
+        """Fine solution u = sum_i w_i phi_i in every cell (msfem_reconstruct);
+        basis in msfem_run_batch's layout, weights [n_cells][2^d]."""
+        keep = []
+        d = self.make_desc(problem, keep=keep)
+        nv = 1 << d.dim
+        b = np.ascontiguousarray(basis, dtype=np.float64).ravel()
+        w = np.ascontiguousarray(weights, dtype=np.float64).ravel()
+        assert b.size == self.basis_size(problem) and w.size == d.n_cells * nv
+        u = np.zeros(b.size // nv)
+        rc = self.lib.msfem_reconstruct(self.handle, ctypes.byref(d), _ptr(b), _ptr(w), _ptr(u))
+        if rc != _abi.OK:
+            raise _abi.MsfemError(rc, _abi.last_error(self.lib))
+        return u
+
     def autotune(self, problem, precision="fp64", tol=1e-10, maxit=1000, sample_cells=1024):
         """Pick the fastest compiled launch shape / parameters for this
         problem's (dim, N class, precision); kept in the handle."""

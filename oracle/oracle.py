@@ -22,6 +22,7 @@ SOLVER_SSOR_CG = 1
 SOLVER_JACOBI_CG = 2
 ORDER_LEX = 0
 ORDER_DEALII = 1
+COEF_TABULATED = 5  # OC_COEF_TABULATED (msfem_oracle.h), = MSFEM_COEF_TABULATED
 
 
 class OcCoef(ctypes.Structure):
@@ -122,6 +123,13 @@ def make_batch(problem, solver=SOLVER_DIRECT, tol=1e-12, tol_absolute=False, max
         keep.append(nf)
         b.n_fine_per_cell = _p(nf)
     c = problem["coef"]
+    if (int(c["kind"]) == COEF_TABULATED and c.get("qp_offset") is None and "n_fine_per_cell" in problem):
+        # uneven N without offsets: packed cell blocks of ncomp 2^d N_c^d
+        # values in cell order (the layout the library reads and writes)
+        nfc = np.asarray(problem["n_fine_per_cell"], dtype=np.int64) ** b.dim
+        blocks = int(c.get("ncomp", 1)) * (1 << b.dim) * nfc
+        c = dict(c)
+        c["qp_offset"] = np.concatenate([[0], np.cumsum(blocks)[:-1]]).astype(np.int64)
     b.coef.kind = int(c["kind"])
     b.coef.ncomp = int(c.get("ncomp", 0))
     for i, v in enumerate(c.get("params", [])):

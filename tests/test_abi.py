@@ -74,6 +74,8 @@ def test_invalid_descriptors_are_rejected_without_a_gpu(built):
     assert lib.msfem_tabulated_size(None, 1) == -1
     rc = lib.msfem_energy_error(None, ctypes.byref(d), None, None, None, None)
     assert rc == abi.ERR_INVALID_ARG
+    rc = lib.msfem_reconstruct(None, ctypes.byref(d), None, None, None)
+    assert rc == abi.ERR_INVALID_ARG
     corners = np.zeros((3, 4, 2))
     d.dim = 2
     d.n_cells = 3
