@@ -195,3 +195,17 @@ def test_every_compiled_launch_shape_gives_the_same_answer(pkg, oracle, engine, 
                 check(got, ref)
     engine.set_tuning({"dim": 2, "n_max": n_max, "precision": prec, "variant": 0, "check_interval": 0,
                        "inner_tol": 1e-6})
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_empty_batch(pkg, engine, dim):
+    """No cells: every entry point returns OK without launching work."""
+    W = pkg.workloads
+    nv = 1 << dim
+    prob = W.problem(dim, np.zeros((0, nv, dim)), np.zeros(0, dtype=np.int32),
+                     {"kind": 2, "params": [0.5, 0.25]})
+    for precision in ("fp64", "mixed"):
+        got = engine.run(prob, precision=precision, want_basis=True)
+        assert got["rc"] == 0
+        assert got["M"].shape == (0, nv, nv) and got["stats"]["solves"] == 0
+    assert engine.reconstruct(prob, np.zeros(0), np.zeros((0, nv))).shape == (0,)
