@@ -258,6 +258,99 @@ __device__ __forceinline__ void stencil27_nm(const float *__restrict__ c, const 
   }
 }
 
+// Half H (RHS 4H .. 4H+3) of a node-major vector at node g: one 16-byte access.
+template <int H>
+__device__ __forceinline__ float4 ldh(const float *__restrict__ v, int g) {
+  return *reinterpret_cast<const float4 *>(v + 8 * (long)g + 4 * H);
+}
+template <int H>
+__device__ __forceinline__ void sth(float *__restrict__ v, int g, float4 t) {
+  *reinterpret_cast<float4 *>(v + 8 * (long)g + 4 * H) = t;
+}
+
+// Index of the forward coupling (dx, dy, dz) among a node's 13 (compile-time
+// offsets; the same order as fwd_offset / cs.offs).
+__host__ __device__ constexpr int fwd_slot(int dx, int dy, int dz) {
+  return dz == 1 ? 4 + (dy + 1) * 3 + (dx + 1) : (dy == 1 ? 1 + (dx + 1) : 0);
+}
+__host__ __device__ constexpr bool fwd_dir(int dx, int dy, int dz) {
+  return dz > 0 || (dz == 0 && (dy > 0 || (dy == 0 && dx > 0)));
+}
+
+// Scaled coupling of node g with its neighbour at (dx, dy, dz) != 0: the
+// node's own forward coupling, or the neighbour's forward coupling back.
+template <int DX, int DY, int DZ>
+__device__ __forceinline__ float coupling_nm(const float *__restrict__ c, long G, int P, int g) {
+  if constexpr (fwd_dir(DX, DY, DZ)) return c[fwd_slot(DX, DY, DZ) * G + g];
+  else return c[fwd_slot(-DX, -DY, -DZ) * G + g + (DZ * P + DY) * P + DX];
+}
+
+// q = A~ p for the z-pair of nodes g0 and g0 + P^2 (RHS 4H .. 4H+3 of the
+// node-major p): the two 27-point stencils share 18 of their 36 neighbour
+// sites, so the pair reads 36 sites instead of 54 (the inner loop is bound
+// by L1 throughput).  Without a second node (two = false) y1, p1 stay 0.
+template <int H, int SZ, int SY, int SX>
+__device__ __forceinline__ void pair_site(const float *__restrict__ c, const float *__restrict__ v, long G,
+                                          int P, int g0, bool two, float4 &y0, float4 &y1, float4 &p0,
+                                          float4 &p1) {
+  constexpr bool use0 = SZ <= 1;
+  const bool use1 = two && SZ >= 0;
+  const float4 t = (use0 || use1) ? ldh<H>(v, g0 + (SZ * P + SY) * P + SX) : make_float4(0.f, 0.f, 0.f, 0.f);
+  if constexpr (use0) {
+    if constexpr (SX == 0 && SY == 0 && SZ == 0) {
+      p0 = t;
+      y0.x += t.x; y0.y += t.y; y0.z += t.z; y0.w += t.w;
+    } else {
+      const float cf = coupling_nm<SX, SY, SZ>(c, G, P, g0);
+      y0.x = fmaf(cf, t.x, y0.x); y0.y = fmaf(cf, t.y, y0.y);
+      y0.z = fmaf(cf, t.z, y0.z); y0.w = fmaf(cf, t.w, y0.w);
+    }
+  }
+  if constexpr (SZ >= 0) {
+    if (use1) {
+      if constexpr (SX == 0 && SY == 0 && SZ == 1) {
+        p1 = t;
+        y1.x += t.x; y1.y += t.y; y1.z += t.z; y1.w += t.w;
+      } else {
+        const float cf = coupling_nm<SX, SY, SZ - 1>(c, G, P, g0 + P * P);
+        y1.x = fmaf(cf, t.x, y1.x); y1.y = fmaf(cf, t.y, y1.y);
+        y1.z = fmaf(cf, t.z, y1.z); y1.w = fmaf(cf, t.w, y1.w);
+      }
+    }
+  }
+}
+template <int H, int SZ, int SY>
+__device__ __forceinline__ void pair_row(const float *__restrict__ c, const float *__restrict__ v, long G, int P,
+                                         int g0, bool two, float4 &y0, float4 &y1, float4 &p0, float4 &p1) {
+  pair_site<H, SZ, SY, -1>(c, v, G, P, g0, two, y0, y1, p0, p1);
+  pair_site<H, SZ, SY, 0>(c, v, G, P, g0, two, y0, y1, p0, p1);
+  pair_site<H, SZ, SY, 1>(c, v, G, P, g0, two, y0, y1, p0, p1);
+}
+template <int H, int SZ>
+__device__ __forceinline__ void pair_plane(const float *__restrict__ c, const float *__restrict__ v, long G, int P,
+                                           int g0, bool two, float4 &y0, float4 &y1, float4 &p0, float4 &p1) {
+  pair_row<H, SZ, -1>(c, v, G, P, g0, two, y0, y1, p0, p1);
+  asm volatile("" ::: "memory");
+  pair_row<H, SZ, 0>(c, v, G, P, g0, two, y0, y1, p0, p1);
+  asm volatile("" ::: "memory");
+  pair_row<H, SZ, 1>(c, v, G, P, g0, two, y0, y1, p0, p1);
+}
+template <int H>
+__device__ __forceinline__ void stencil27_pair(const float *__restrict__ c, const float *__restrict__ v, long G,
+                                               int P, int g0, bool two, float4 &y0, float4 &y1, float4 &p0,
+                                               float4 &p1) {
+  y0 = y1 = p0 = p1 = make_float4(0.f, 0.f, 0.f, 0.f);
+  // one row of sites' loads in flight at a time (the empty asm statements
+  // keep the compiler from hoisting all 36 sites' loads, which would spill)
+  pair_plane<H, -1>(c, v, G, P, g0, two, y0, y1, p0, p1);
+  asm volatile("" ::: "memory");
+  pair_plane<H, 0>(c, v, G, P, g0, two, y0, y1, p0, p1);
+  asm volatile("" ::: "memory");
+  pair_plane<H, 1>(c, v, G, P, g0, two, y0, y1, p0, p1);
+  asm volatile("" ::: "memory");
+  pair_plane<H, 2>(c, v, G, P, g0, two, y0, y1, p0, p1);
+}
+
 __device__ __forceinline__ int grid3(int P, int ix, int iy, int iz) { return ((iz + 1) * P + iy + 1) * P + ix + 1; }
 
 // Geometry and Q1 data of one cell: corners, coupling offsets, BasisQ1
@@ -366,7 +459,7 @@ __device__ __forceinline__ T *peer(T *ptr, int rank) {
 // once per segment rather than held in registers through the FP32 loop (the
 // 2-CTA/SM shapes run at 64 registers per thread).  Reductions use red[buf],
 // red[buf ^ 1] alternately, buf as left by the caller's last reduction.
-template <int NT, int CS>
+template <int NT, int CS, int PC>
 __device__ __noinline__ void inner_segment3d(const float *__restrict__ c32, float *pp32, float *qq32,
                                              float *rr32, float *dd32, long G, int m, int P, int nI,
                                              int inner_maxit, unsigned iact, int buf,
@@ -409,13 +502,41 @@ __device__ __noinline__ void inner_segment3d(const float *__restrict__ c32, floa
     float sg[8];
 #pragma unroll
     for (int r = 0; r < 8; ++r) sg[r] = 0.f;
-    for (int k = ctid; k < nI; k += CNT) {
-      const int g = interior(k);
-      float y[8], pc[8];
-      stencil27_nm(c32, pp32, G, cs.offs, g, y, pc);
-      st8(qq32, g, y);
+    if constexpr (PC == 0) {
+      // any N: one node (8 RHS) per thread
+      for (int k = ctid; k < nI; k += CNT) {
+        const int g = interior(k);
+        float y[8], pc[8];
+        stencil27_nm(c32, pp32, G, cs.offs, g, y, pc);
+        st8(qq32, g, y);
 #pragma unroll
-      for (int r = 0; r < 8; ++r) sg[r] = fmaf(pc[r], y[r], sg[r]);
+        for (int r = 0; r < 8; ++r) sg[r] = fmaf(pc[r], y[r], sg[r]);
+      }
+    } else {
+    // q = A~ p and p.q over z-pairs of interior nodes (iz, iz + 1), iz odd;
+    // with m odd the last layer holds single nodes.  P = PC is a compile-
+    // time constant here, so the 36 site offsets are immediates.
+    constexpr int P = PC, m = PC - 4, mz = (m + 1) / 2;
+    for (int k = ctid; k < m * m * mz; k += CNT) {
+      const int ix = 1 + k % m, iy = 1 + (k / m) % m, iz = 1 + 2 * (k / (m * m));
+      const bool two = iz < m;
+      const int g0 = grid3(P, ix, iy, iz);
+      float4 y0, y1, p0, p1;
+      stencil27_pair<0>(c32, pp32, G, P, g0, two, y0, y1, p0, p1);
+      sth<0>(qq32, g0, y0);
+      if (two) sth<0>(qq32, g0 + P * P, y1);
+      sg[0] = fmaf(p0.x, y0.x, fmaf(p1.x, y1.x, sg[0]));
+      sg[1] = fmaf(p0.y, y0.y, fmaf(p1.y, y1.y, sg[1]));
+      sg[2] = fmaf(p0.z, y0.z, fmaf(p1.z, y1.z, sg[2]));
+      sg[3] = fmaf(p0.w, y0.w, fmaf(p1.w, y1.w, sg[3]));
+      stencil27_pair<1>(c32, pp32, G, P, g0, two, y0, y1, p0, p1);
+      sth<1>(qq32, g0, y0);
+      if (two) sth<1>(qq32, g0 + P * P, y1);
+      sg[4] = fmaf(p0.x, y0.x, fmaf(p1.x, y1.x, sg[4]));
+      sg[5] = fmaf(p0.y, y0.y, fmaf(p1.y, y1.y, sg[5]));
+      sg[6] = fmaf(p0.z, y0.z, fmaf(p1.z, y1.z, sg[6]));
+      sg[7] = fmaf(p0.w, y0.w, fmaf(p1.w, y1.w, sg[7]));
+    }
     }
     block_sum8(sg);
     float al[8], rp[8];
@@ -1017,7 +1138,15 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
           cs.seg_rho[0][tid] = q;
         }
         __syncthreads();
-        inner_segment3d<NT, CS>(c32, pp32, qq32, rr32, dd32, G, m, P, nI, p.inner_maxit, iact, buf, red, cs);
+        // the config-4 sizes get the z-pair stencil with compile-time offsets
+        if (N == 24)
+          inner_segment3d<NT, CS, 27>(c32, pp32, qq32, rr32, dd32, G, m, P, nI, p.inner_maxit, iact, buf, red, cs);
+        else if (N == 16)
+          inner_segment3d<NT, CS, 19>(c32, pp32, qq32, rr32, dd32, G, m, P, nI, p.inner_maxit, iact, buf, red, cs);
+        else if (N == 8)
+          inner_segment3d<NT, CS, 11>(c32, pp32, qq32, rr32, dd32, G, m, P, nI, p.inner_maxit, iact, buf, red, cs);
+        else
+          inner_segment3d<NT, CS, 0>(c32, pp32, qq32, rr32, dd32, G, m, P, nI, p.inner_maxit, iact, buf, red, cs);
         // x~ += d (FP64); r = -(A~ phi~)_I in FP64
         for (int k = ctid; k < nI; k += CNT) {
           const int g = interior(k);
