@@ -517,19 +517,20 @@ __device__ __noinline__ void inner_segment3d(const float *__restrict__ c32, floa
     // with m odd the last layer holds single nodes.  P = PC is a compile-
     // time constant here, so the 36 site offsets are immediates.
     constexpr int P = PC, m = PC - 4, mz = (m + 1) / 2;
+    constexpr long GC = (long)PC * PC * PC;  // = G: coupling offsets are immediates too
     for (int k = ctid; k < m * m * mz; k += CNT) {
       const int ix = 1 + k % m, iy = 1 + (k / m) % m, iz = 1 + 2 * (k / (m * m));
       const bool two = iz < m;
       const int g0 = grid3(P, ix, iy, iz);
       float4 y0, y1, p0, p1;
-      stencil27_pair<0>(c32, pp32, G, P, g0, two, y0, y1, p0, p1);
+      stencil27_pair<0>(c32, pp32, GC, P, g0, two, y0, y1, p0, p1);
       sth<0>(qq32, g0, y0);
       if (two) sth<0>(qq32, g0 + P * P, y1);
       sg[0] = fmaf(p0.x, y0.x, fmaf(p1.x, y1.x, sg[0]));
       sg[1] = fmaf(p0.y, y0.y, fmaf(p1.y, y1.y, sg[1]));
       sg[2] = fmaf(p0.z, y0.z, fmaf(p1.z, y1.z, sg[2]));
       sg[3] = fmaf(p0.w, y0.w, fmaf(p1.w, y1.w, sg[3]));
-      stencil27_pair<1>(c32, pp32, G, P, g0, two, y0, y1, p0, p1);
+      stencil27_pair<1>(c32, pp32, GC, P, g0, two, y0, y1, p0, p1);
       sth<1>(qq32, g0, y0);
       if (two) sth<1>(qq32, g0 + P * P, y1);
       sg[4] = fmaf(p0.x, y0.x, fmaf(p1.x, y1.x, sg[4]));
