@@ -469,9 +469,17 @@ __device__ __noinline__ void inner_segment3d(const float *__restrict__ c32, floa
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int ctid = cluster_rank<CS>() * NT + tid;
   auto interior = [&](int k) {
-    const int ix = 1 + k % m, iy = 1 + (k / m) % m, iz = 1 + k / (m * m);
-    return grid3(P, ix, iy, iz);
+    if constexpr (PC > 0) {
+      // compile-time m and P: the divisions become multiplications
+      constexpr int mc = PC - 4;
+      const int ix = 1 + k % mc, iy = 1 + (k / mc) % mc, iz = 1 + k / (mc * mc);
+      return grid3(PC, ix, iy, iz);
+    } else {
+      const int ix = 1 + k % m, iy = 1 + (k / m) % m, iz = 1 + k / (m * m);
+      return grid3(P, ix, iy, iz);
+    }
   };
+
   auto block_sum8 = [&](float (&v)[8]) {
     float vv[8];
 #pragma unroll
