@@ -184,7 +184,7 @@ def run_reference_arm(args):
     oracle = graft.load_oracle()
     oracle.build()
     W = pkg.workloads
-    full = W.config2(K=K_COARSE, N=N_FINE)
+    full = W.fourier_square(K=K_COARSE, N=N_FINE)
     nthreads = os.cpu_count() or 1
     n_sample = max(16, min(4096, 64 * nthreads))
     cells = np.linspace(0, K_COARSE * K_COARSE - 1, n_sample).astype(int)
@@ -224,9 +224,9 @@ def main():
     ap.add_argument("--variant", type=int, default=None, help="--profile: launch shape index to use")
     ap.add_argument("--inner-tol", type=float, default=1e-6, help="--profile 2D mixed: inner FP32 reduction")
     ap.add_argument("--cheb-ratio", type=float, default=30.0, help="--profile 2D mixed: Chebyshev interval ratio")
-    ap.add_argument("--no-config3", action="store_true", help="skip the 65536-cell config-3 timing")
+    ap.add_argument("--no-fourier-256", action="store_true", help="skip the 256x256-cell (65536) Fourier-field timing")
     ap.add_argument("--no-surrogate", action="store_true", help="skip training / evaluating the warm start")
-    ap.add_argument("--no-config4", action="store_true", help="skip the 3D uneven-N config-4 timing")
+    ap.add_argument("--no-spheres-3d", action="store_true", help="skip the 3D uneven-N sphere-field timing")
     ap.add_argument("--coarse", type=int, default=K_COARSE, help="coarse cells per direction")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -367,7 +367,7 @@ def main():
         t_ms = None
         if kind in ("fp64_2d", "mixed_2d"):
             # 48x48 cells: a 226 MB tabulated field, larger than L2
-            wsp = make_ws(W.config2(K=48, N=N_FINE), 0)
+            wsp = make_ws(W.fourier_square(K=48, N=N_FINE), 0)
             prec = abi.PREC_FP64 if kind == "fp64_2d" else abi.PREC_MIXED
             if args.variant is not None:
                 eng.set_tuning({"dim": 2, "n_max": N_FINE, "precision": prec, "variant": args.variant,
@@ -375,8 +375,8 @@ def main():
                                 "cheb_ratio": args.cheb_ratio})
             t_ms, _, _ = timed_ws(wsp, prec, args.steps, args.warmup)
         elif kind in ("fp64_3d", "mixed_3d"):
-            # the first 256 cells of config 4 (uneven N, 1e4-contrast spheres)
-            sub = W.subset(W.config4(), np.arange(256))
+            # the first 256 cells of the 3D sphere field (uneven N, 1e4-contrast spheres)
+            sub = W.subset(W.spheres_cube(), np.arange(256))
             prec = "fp64" if kind == "fp64_3d" else "mixed"
             if args.variant is not None:
                 eng.set_tuning({"dim": 3, "n_max": 24, "precision": 0 if prec == "fp64" else 1,
@@ -389,7 +389,7 @@ def main():
         elif kind == "cnn":
             # inference of 2048 cells and training steps of batch 256 (random weights)
             S = pkg.surrogate
-            desc_p, keep_p = S.device_problem(eng, W.subset(W.config2(K=64, N=N_FINE), np.arange(2048)), torch)
+            desc_p, keep_p = S.device_problem(eng, W.subset(W.fourier_square(K=64, N=N_FINE), np.arange(2048)), torch)
             feats = S.features(eng, desc_p, torch)
             sur = S.Surrogate(eng, seed=7)
             out = torch.empty((2048, 4, 33, 33), dtype=torch.float32, device=f"cuda:{local}")
@@ -415,7 +415,7 @@ def main():
 
     # ---- workload on the device (weak scaling: every rank owns its own
     # 64x64 block of coarse cells, shifted by the rank along x)
-    prob = W.config2(K=args.coarse, N=N_FINE)
+    prob = W.fourier_square(K=args.coarse, N=N_FINE)
     ws2 = make_ws(prob, rank)
     n_cells, size, corners_h = ws2["n"], ws2["size"], ws2["corners_h"]
     solves_rank = 4 * n_cells
@@ -448,7 +448,7 @@ def main():
     achieved = flops64 / (ms64 * 1e-3) / 1e12
     peaks, peak_src = read_peaks()
     alg_bytes = size * 8 + n_cells * (8 * 2 * 4 + 8 * 20 + 4 * 5)  # field + corners + outputs
-    traffic = read_profile_traffic("msfem2d_fp64_config2.txt")
+    traffic = read_profile_traffic("msfem2d_fp64_fourier64x64.txt")
     roofline = {
         "bound": "fp64", "achieved": achieved, "peak": fp64_peak.value / 1e12, "unit": "TFLOP/s",
         "frac": achieved / (fp64_peak.value / 1e12),
@@ -549,14 +549,14 @@ def main():
             line["mixed"]["e2e"] = {"value": world * solves_rank / e2e_m, "unit": UNIT, "ms_per_step": e2e_m * 1e3,
                                     "h2d_bytes_per_step": line["e2e"]["h2d_bytes_per_step"],
                                     "d2h_bytes_per_step": line["e2e"]["d2h_bytes_per_step"]}
-    # ---- config 3 workload: 256x256 coarse cells (65536), mixed vs FP64
-    if not args.no_config3 and world == 1 and args.coarse == K_COARSE:
-        ws3 = make_ws(W.config3(), 0)
+    # ---- 256x256 coarse cells (65536) of the evaluation Fourier field, mixed vs FP64
+    if not args.no_fourier_256 and world == 1 and args.coarse == K_COARSE:
+        ws3 = make_ws(W.fourier_square(K=256, N=32, seeds=W.EVAL_SEEDS), 0)
         st3 = max(2, min(5, args.steps))
         ms3m, s3m, _ = timed_ws(ws3, abi.PREC_MIXED, st3, 3)
         ms3f, s3f, _ = timed_ws(ws3, abi.PREC_FP64, 2, 3)
         n3 = ws3["n"]
-        line["config3"] = {
+        line["fourier_256x256"] = {
             "workload": "2D 256x256 coarse cells, 32x32 fine Q1, 4 RHS, random-Fourier SPD tensor "
                         "(seeds 3/30/300), f=1, 1e-10 rel residual",
             "mixed": {"value": 4 * n3 / (ms3m * 1e-3), "unit": UNIT, "ms_per_step": ms3m,
@@ -568,14 +568,14 @@ def main():
                      "max_rel_residual": s3f["max_rel_residual"], "cells_failed": s3f["cells_failed"]},
             "speedup_mixed_vs_fp64": ms3f / ms3m,
         }
-        line["gpu_launches_config3"] = st3 + 2
+        line["gpu_launches_fourier_256x256"] = st3 + 2
         # per-basis energy-norm and coarse-matrix errors of every cell against
         # the FP64 form solved to 1e-12 (untimed)
         ref3 = solve_with_basis(ws3, abi.PREC_FP64, 1e-12)
         errs = {}
         for prec, pname in ((abi.PREC_MIXED, "mixed"), (abi.PREC_FP64, "fp64")):
             errs[pname] = basis_errors(ws3, solve_with_basis(ws3, prec, TOL), ref3)
-        line["config3"]["errors_vs_fp64_1e-12"] = {
+        line["fourier_256x256"]["errors_vs_fp64_1e-12"] = {
             "reference": "FP64 form solved to 1e-12 relative residual, same cells and field; "
                          "energy norm ||phi - phi_ref||_A / ||phi_ref||_A per basis function, "
                          "coarse entries |M_ij - M_ref,ij| / max_ij |M_ref,ij| per cell",
@@ -584,12 +584,12 @@ def main():
         if args.no_surrogate:
             del ref3
         torch.cuda.empty_cache()
-    # ---- config 4: 3D unit cube, 16^3 coarse cells with uneven N in {8,16,24},
+    # ---- 3D unit cube, 16^3 coarse cells with uneven N in {8,16,24},
     # 1e4-contrast spheres, 8 RHS; one persistent kernel per call, autotuned
     # on a sample of the batch, FP64 and mixed
-    if not args.no_config4 and world == 1 and args.coarse == K_COARSE:
+    if not args.no_spheres_3d and world == 1 and args.coarse == K_COARSE:
         t0 = time.time()
-        prob4 = W.config4()
+        prob4 = W.spheres_cube()
         t_rsa = time.time() - t0
         nc4 = prob4["corners"].shape[0]
         nf4_h = np.ascontiguousarray(prob4["n_fine_per_cell"], dtype=np.int32)
@@ -666,12 +666,12 @@ def main():
             res4[pname]["cg_frac_of_measured_" + ("fp64" if prec == abi.PREC_FP64 else "fp32") + "_peak"] = \
                 flw / (ms * 1e-3) / peak
         res4["speedup_mixed_vs_fp64"] = res4["fp64"]["ms_per_step"] / res4["mixed"]["ms_per_step"]
-        line["config4"] = res4
+        line["spheres_3d"] = res4
         del tab4, M4, F4, st4, it4, corners4, nf4
         torch.cuda.empty_cache()
     # ---- learned warm start (the surrogate): trained here with the library's
     # own BF16 tensor-core forward/backward kernels, evaluated on the unseen
-    # config-3 field (65536 cells) against the cold start
+    # 256x256-cell evaluation field (65536 cells) against the cold start
     if not args.no_surrogate and world == 1 and args.coarse == K_COARSE:
         S = pkg.surrogate
         t0 = time.time()
@@ -684,7 +684,7 @@ def main():
         torch.cuda.synchronize()
         t_train = time.time() - t0
         del feats, tgts
-        desc5, keep5 = S.device_problem(eng, W.config3(), torch)
+        desc5, keep5 = S.device_problem(eng, W.fourier_square(K=256, N=32, seeds=W.EVAL_SEEDS), torch)
         ev = {}
         for prec, pname in ((abi.PREC_MIXED, "mixed"), (abi.PREC_FP64, "fp64")):
             for warm, wname in ((abi.WARM_NONE, "cold"), (abi.WARM_SURROGATE, "surrogate")):
@@ -705,7 +705,7 @@ def main():
                     "value": st["solves"] / (ms * 1e-3), "unit": UNIT, "ms": ms,
                     "mean_iterations": st["iterations_total"] / st["solves"],
                     "max_rel_residual": st["max_rel_residual"], "cells_failed": st["cells_failed"]}
-        if not args.no_config3:
+        if not args.no_fourier_256:
             sur.attach()
             for prec, pname in ((abi.PREC_MIXED, "mixed"), (abi.PREC_FP64, "fp64")):
                 got = solve_with_basis(None, prec, TOL, warm=abi.WARM_SURROGATE, desc=desc5)
@@ -725,7 +725,7 @@ def main():
             "training": {"solves": int(4 * 12 * 4096), "epochs": 20, "batch": 256,
                          "data_seconds": t_data, "train_seconds": t_train,
                          "loss_first_epoch": hist[0], "loss_last_epoch": hist[-1]},
-            "eval_workload": "config 3 field (seeds 3/30/300, not in the training set), 65536 cells",
+            "eval_workload": "256x256-cell random-Fourier field (seeds 3/30/300, not in the training set), 65536 cells",
             "results": ev,
         }
         sur.close()

@@ -1147,7 +1147,8 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
           cs.seg_rho[0][tid] = q;
         }
         __syncthreads();
-        // the config-4 sizes get the z-pair stencil with compile-time offsets
+        // N = 8, 16, 24 (the uneven 3D sphere workload) get the z-pair stencil
+        // with compile-time offsets
         if (N == 24)
           inner_segment3d<NT, CS, 27>(c32, pp32, qq32, rr32, dd32, G, m, P, nI, p.inner_maxit, iact, buf, red, cs);
         else if (N == 16)

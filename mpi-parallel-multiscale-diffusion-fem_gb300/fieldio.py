@@ -18,8 +18,9 @@ File layout (little-endian, every section 8-byte aligned):
   ...     f64 [sum_c ncomp 2^d N_c^d]        the field: per cell
                                              [component][Gauss point][fine cell]
 
-The payload is read with numpy.memmap, so a multi-GB field (config 3: 6.4 GB)
-is not copied on load; pinned or device staging is the caller's choice.
+The payload is read with numpy.memmap, so a multi-GB field (256 x 256 cells,
+N = 32, 3 components: 6.4 GB) is not copied on load; pinned or device staging
+is the caller's choice.
 """
 import numpy as np
 

@@ -136,13 +136,13 @@ def solve_device(engine, desc, torch, precision=_abi.PREC_MIXED, want_basis=Fals
 
 
 def training_set(engine, torch, seeds=None, K=64, log=None):
-    """Basis solves of random-Fourier tensor fields (the config-2 family with
+    """Basis solves of random-Fourier tensor fields (the fourier_square family with
     new seeds): features and targets delta = phi - Q1 on the device."""
     seeds = seeds or [(100 + 7 * i, 1000 + 7 * i, 10000 + 7 * i) for i in range(12)]
     feats, tgts = [], []
     for sd in seeds:
         t0 = time.time()
-        prob = workloads.config2(K=K, N=32, seeds=sd)
+        prob = workloads.fourier_square(K=K, N=32, seeds=sd)
         desc, keep = device_problem(engine, prob, torch)
         res = solve_device(engine, desc, torch, want_basis=True)
         assert res["stats"]["cells_failed"] == 0

@@ -141,28 +141,31 @@ def reference_problem(dim=2, n_refine=3, n_refine_local=4):
                    {"kind": _abi.COEF_REFERENCE}, f_value=2.0)
 
 
-def config1():
-    """2D 8x8 coarse, N = 16, a = 1 + 0.9 sin(2 pi x/eps) sin(2 pi y/eps),
-    eps = 1/64, f = 1 (homogeneous Dirichlet on the global boundary)."""
-    return problem(2, unit_cube_corners(2, 8), 16,
+def sinsin_square(K=8, N=16):
+    """2D unit square, K x K coarse cells, N = 16, a = 1 + 0.9 sin(2 pi x/eps)
+    sin(2 pi y/eps), eps = 1/64, f = 1 (homogeneous Dirichlet on the global
+    boundary)."""
+    return problem(2, unit_cube_corners(2, K), N,
                    {"kind": _abi.COEF_SINSIN, "params": [0.9, 1.0 / 64]}, f_value=1.0)
 
 
-def config2(K=64, N=32, seeds=(2, 20, 200)):
-    """2D 64x64 coarse, N = 32, random-Fourier SPD tensor (seeds 2/20/200), f = 1."""
+# seeds (g1, g2, theta) of the random-Fourier tensor fields: the 64 x 64
+# throughput field, and the 256 x 256 evaluation field of the mixed form and
+# the warm start (never used for training)
+FOURIER_SEEDS = (2, 20, 200)
+EVAL_SEEDS = (3, 30, 300)
+
+
+def fourier_square(K=64, N=32, seeds=FOURIER_SEEDS):
+    """2D unit square, K x K coarse cells, N fine cells per direction, the
+    random-Fourier SPD tensor a = R(theta) diag(e^g1, e^g2) R(theta)^T, f = 1."""
     return problem(2, unit_cube_corners(2, K), N, fourier_coef(seeds), f_value=1.0)
 
 
-def config3(K=256, N=32, seeds=(3, 30, 300)):
-    """2D 256x256 coarse, N = 32, the config-2 random-Fourier family with new
-    seeds 3/30/300, f = 1 (mixed-precision workload)."""
-    return problem(2, unit_cube_corners(2, K), N, fourier_coef(seeds), f_value=1.0)
-
-
-def config4(K=16, seed=4, sphere_seed=44, sizes=(8, 16, 24), contrast=1e4, spheres=None):
-    """3D 16^3 coarse, N per cell drawn uniformly from `sizes`, background 1 plus
-    non-overlapping spheres (r in [0.004, 0.012], volume fraction 0.2) of
-    value `contrast`, f = 1."""
+def spheres_cube(K=16, seed=4, sphere_seed=44, sizes=(8, 16, 24), contrast=1e4, spheres=None):
+    """3D unit cube, K^3 coarse cells, N per cell drawn uniformly from `sizes`,
+    background 1 plus non-overlapping spheres (r in [0.004, 0.012], volume
+    fraction 0.2) of value `contrast`, f = 1."""
     rng = SplitMix64(seed)
     n_cells = K ** 3
     nf = np.array([sizes[int(rng.uniform() * len(sizes)) % len(sizes)] for _ in range(n_cells)],

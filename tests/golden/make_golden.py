@@ -9,13 +9,13 @@ coarse problem, and fingerprints of the generated inputs (corners, Fourier
 modes) so a test can tell a changed input generator from a changed solver.
 
 Cases:
-  config1          2D 8x8 coarse, N = 16, a = 1 + 0.9 sin(2 pi x/eps) sin(2 pi y/eps),
+  sinsin_8x8       2D 8x8 coarse, N = 16, a = 1 + 0.9 sin(2 pi x/eps) sin(2 pi y/eps),
                    eps = 1/64, f = 1; coarse solve with homogeneous Dirichlet data
   reference_2d     the reference's own problem (MatrixCoeff with PI_D, f = 2,
                    Dirichlet ids 0/2, Neumann ids 1/3) at n_refine = 3,
                    n_refine_local = 4 (source/main.cxx), with the coarse solution
   reference_3d     the same in 3D at n_refine = 1, n_refine_local = 2
-  config2_cells    six cells of the config-2 random-Fourier tensor field
+  fourier_cells    six cells of the random-Fourier tensor field
                    (64x64 coarse, N = 32, seeds 2/20/200)
   uneven_3d        five 3D cells with N in {1, 2, 3, 5, 4}, scalar sin-sin coefficient
 """
@@ -44,10 +44,10 @@ def cases(W):
     uneven = W.problem(3, W.unit_cube_corners(3, 2)[:5], np.array([1, 2, 3, 5, 4], dtype=np.int32),
                        {"kind": 2, "params": [0.5, 0.25]}, f_value=1.5)
     return {
-        "config1": (W.config1(), (2, 8, 1)),
+        "sinsin_8x8": (W.sinsin_square(), (2, 8, 1)),
         "reference_2d": (W.reference_problem(2, 3, 4), (2, 8, 0)),
         "reference_3d": (W.reference_problem(3, 1, 2), (3, 2, 0)),
-        "config2_cells": (W.subset(W.config2(K=64, N=32), [0, 1, 63, 64, 2080, 4095]), None),
+        "fourier_cells": (W.subset(W.fourier_square(K=64, N=32), [0, 1, 63, 64, 2080, 4095]), None),
         "uneven_3d": (uneven, None),
     }
 

@@ -30,10 +30,10 @@ def check_against_oracle(engine, oracle, prob, basis, ref_basis):
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_energy_error_2d_against_oracle(pkg, oracle, engine, precision):
-    """Random-Fourier tensor (config-2 family, tabulated path), N = 32: the
+    """Random-Fourier tensor (fourier_square family, tabulated path), N = 32: the
     GPU basis solved to 1e-10 against the oracle's direct solve."""
     W = pkg.workloads
-    prob = W.subset(W.config2(K=64, N=32), [0, 17, 2080, 4095])
+    prob = W.subset(W.fourier_square(K=64, N=32), [0, 17, 2080, 4095])
     got = engine.run(prob, precision=precision, tol=1e-10, want_basis=True)
     ref = oracle.run(prob, want_basis=True)
     err, nrm, live = check_against_oracle(engine, oracle, prob, got["basis"], ref["basis"])
@@ -82,7 +82,7 @@ def test_energy_error_general_geometry(pkg, oracle, engine, geom):
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_energy_error_3d_uneven_spheres(pkg, oracle, engine, precision):
-    """Config-4 style: 1e4-contrast spheres, uneven N in one call."""
+    """1e4-contrast spheres, uneven N in one call."""
     W = pkg.workloads
     rng = np.random.default_rng(5)
     sp = np.column_stack([rng.uniform(0, 1, (600, 3)), rng.uniform(0.02, 0.05, 600)])
@@ -112,7 +112,7 @@ def test_energy_error_device_memory(pkg, oracle, engine):
 
     W = pkg.workloads
     abi = pkg._abi
-    prob = W.subset(W.config2(K=64, N=32), [3, 9])
+    prob = W.subset(W.fourier_square(K=64, N=32), [3, 9])
     got = engine.run(prob, precision="mixed", tol=1e-10, want_basis=True)
     ref = oracle.run(prob, want_basis=True)
     err_h, nrm_h = engine.energy_error(prob, got["basis"], ref["basis"])

@@ -12,7 +12,7 @@ def _field(pkg, oracle, uneven):
         corners = W.unit_cube_corners(2, 4)[[0, 3, 9, 14]]
         prob = W.problem(2, corners, np.array([4, 8, 2, 6], dtype=np.int32), {"kind": 2, "params": [0.9, 0.25]})
     else:
-        prob = W.subset(W.config2(K=64, N=32), [0, 77, 4095])
+        prob = W.subset(W.fourier_square(K=64, N=32), [0, 77, 4095])
         prob = dict(prob)
         prob["n_fine"] = 8  # small N keeps the oracle fast
     return prob, oracle.tabulate(prob, 3)

@@ -1,7 +1,7 @@
 """Parity at the benchmark workloads' own sizes.
 
-Cells taken from the full config-3 field (256x256 coarse, N = 32) and from
-the full config-4 sphere field (112k spheres, N in {8, 16, 24}) against the
+Cells taken from the full 256x256-cell evaluation Fourier field (N = 32) and
+from the full 3D sphere field (112k spheres, N in {8, 16, 24}) against the
 oracle's direct solves (1e-10 relative, M and F); and, over whole batches,
 the size-independent properties of the coarse element matrices: symmetry,
 zero row sums (the basis is a partition of unity), positive
@@ -32,14 +32,14 @@ def check_invariants(M, F, f_total, tol_rows, tol_f):
 
 
 @pytest.fixture(scope="module")
-def config4_field(pkg):
-    return pkg.workloads.config4()
+def sphere_field(pkg):
+    return pkg.workloads.spheres_cube()
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_config3_cells_against_oracle(pkg, oracle, engine, precision):
+def test_fourier_256_cells_against_oracle(pkg, oracle, engine, precision):
     W = pkg.workloads
-    full = W.config3()
+    full = W.fourier_square(K=256, N=32, seeds=W.EVAL_SEEDS)
     prob = W.subset(full, [0, 12345, 40000, 65535])
     got = engine.run(prob, precision=precision, tol=1e-12)
     ref = oracle.run(prob)
@@ -49,11 +49,11 @@ def test_config3_cells_against_oracle(pkg, oracle, engine, precision):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_config4_cells_against_oracle(pkg, oracle, engine, config4_field, precision):
+def test_sphere_cells_against_oracle(pkg, oracle, engine, sphere_field, precision):
     W = pkg.workloads
-    nf = config4_field["n_fine_per_cell"]
+    nf = sphere_field["n_fine_per_cell"]
     cells = [int(np.flatnonzero(nf == v)[0]) for v in (24, 16, 8)] + [int(np.flatnonzero(nf == 24)[-1])]
-    prob = W.subset(config4_field, cells)
+    prob = W.subset(sphere_field, cells)
     got = engine.run(prob, precision=precision, tol=1e-12)
     ref = oracle.run(prob)
     assert got["rc"] == 0 and np.all(got["status"] == 0)
@@ -61,8 +61,8 @@ def test_config4_cells_against_oracle(pkg, oracle, engine, config4_field, precis
     assert rel_err(got["F"], ref["F"]) < 1e-10
 
 
-def test_config2_full_batch_invariants(pkg, engine):
-    prob = pkg.workloads.config2(K=64, N=32)
+def test_fourier_64_full_batch_invariants(pkg, engine):
+    prob = pkg.workloads.fourier_square(K=64, N=32)
     got = engine.run(prob, precision="fp64", tol=1e-10)
     assert got["rc"] == 0 and np.all(got["status"] == 0)
     check_invariants(got["M"], got["F"], 1.0, 1e-9, 1e-9)  # f = 1 on the unit square
@@ -72,7 +72,7 @@ def test_config2_full_batch_invariants(pkg, engine):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_config4_full_batch_invariants(pkg, engine, config4_field, precision):
-    got = engine.run(config4_field, precision=precision, tol=1e-10)
+def test_sphere_full_batch_invariants(pkg, engine, sphere_field, precision):
+    got = engine.run(sphere_field, precision=precision, tol=1e-10)
     assert got["rc"] == 0 and np.all(got["status"] == 0)
     check_invariants(got["M"], got["F"], 1.0, 1e-9, 1e-6)  # f = 1 on the unit cube

@@ -29,8 +29,8 @@ def check(got, ref, basis=True):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_config1_parity(pkg, oracle, engine, precision):
-    prob = pkg.workloads.config1()
+def test_sinsin_square_parity(pkg, oracle, engine, precision):
+    prob = pkg.workloads.sinsin_square()
     got = engine.run(prob, precision=precision, tol=1e-13, want_basis=True)
     ref = oracle.run(prob, want_basis=True)
     check(got, ref)
@@ -56,9 +56,9 @@ def test_fp64_iterations_match_oracle_jacobi_pcg(pkg, oracle, engine):
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_random_fourier_tensor_parity(pkg, oracle, engine, precision):
-    """Config-2 coefficient family on a subset of cells, N = 32, tabulated on the GPU."""
+    """Random-Fourier tensor family on a subset of cells, N = 32, tabulated on the GPU."""
     W = pkg.workloads
-    full = W.config2(K=64, N=32)
+    full = W.fourier_square(K=64, N=32)
     prob = W.subset(full, [0, 1, 63, 64, 2080, 4095])
     got = engine.run(prob, precision=precision, tol=1e-13, want_basis=True)
     # oracle evaluates the same Fourier field itself
@@ -68,7 +68,7 @@ def test_random_fourier_tensor_parity(pkg, oracle, engine, precision):
 
 def test_tabulation_matches_oracle(pkg, oracle, engine):
     W = pkg.workloads
-    prob = W.subset(W.config2(K=64, N=32), [5, 700])
+    prob = W.subset(W.fourier_square(K=64, N=32), [5, 700])
     a = engine.tabulate(prob, 3)
     b = oracle.tabulate(prob, 3)
     assert np.abs(a - b).max() < 1e-12 * np.abs(b).max()
@@ -123,7 +123,7 @@ def test_uneven_refinement_one_launch(pkg, oracle, engine):
 
 
 def test_warm_start_exact_basis_converges_immediately(pkg, oracle, engine):
-    prob = pkg.workloads.config1()
+    prob = pkg.workloads.sinsin_square()
     ref = oracle.run(prob, want_basis=True)
     got = engine.run(prob, precision="fp64", tol=1e-10, want_basis=True, warm_basis=ref["basis"])
     check(got, ref)
@@ -131,7 +131,7 @@ def test_warm_start_exact_basis_converges_immediately(pkg, oracle, engine):
 
 
 def test_maxit_reported_per_cell(pkg, engine):
-    prob = pkg.workloads.config1()
+    prob = pkg.workloads.sinsin_square()
     got = engine.run(prob, precision="fp64", tol=1e-13, maxit=3)
     assert got["rc"] != 0
     assert np.all(got["status"] == pkg._abi.CELL_MAXIT)
@@ -162,7 +162,7 @@ def test_degenerate_cell_reported(pkg, engine):
 
 def test_mixed_reaches_tolerance_and_matches_fp64(pkg, engine):
     W = pkg.workloads
-    prob = W.subset(W.config2(K=64, N=32), list(range(0, 4096, 97)))
+    prob = W.subset(W.fourier_square(K=64, N=32), list(range(0, 4096, 97)))
     a = engine.run(prob, precision="fp64", tol=1e-10)
     b = engine.run(prob, precision="mixed", tol=1e-10)
     assert a["stats"]["max_rel_residual"] < 1e-10
@@ -177,9 +177,9 @@ def test_every_compiled_launch_shape_gives_the_same_answer(pkg, oracle, engine, 
     polynomial-preconditioned shapes, each Chebyshev interval ratio) keeps parity."""
     W = pkg.workloads
     if n_max == 32:
-        prob = W.subset(W.config2(K=64, N=32), [3, 1000, 2222, 4000])
+        prob = W.subset(W.fourier_square(K=64, N=32), [3, 1000, 2222, 4000])
     else:
-        prob = W.subset(W.config1(), [0, 9, 36, 63])
+        prob = W.subset(W.sinsin_square(), [0, 9, 36, 63])
     ref = oracle.run(prob, want_basis=True)
     probe = engine.autotune(prob, precision=precision, tol=1e-13, sample_cells=4)
     assert probe["n_variants"] >= 1

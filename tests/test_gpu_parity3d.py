@@ -57,7 +57,7 @@ def test_ragged_sizes_3d(pkg, oracle, engine, N):
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_spheres_uneven_one_launch(pkg, oracle, engine, precision):
-    """Config-4 coefficient (1e4-contrast spheres) with uneven N in one launch."""
+    """The sphere coefficient (1e4 contrast) with uneven N in one launch."""
     W = pkg.workloads
     rng = np.random.default_rng(5)
     sp = np.column_stack([rng.uniform(0, 1, (600, 3)), rng.uniform(0.02, 0.05, 600)])

@@ -16,7 +16,7 @@ def test_pinned_table_is_read_in_place(pkg, engine, precision):
     torch = pytest.importorskip("torch")
     abi, W = pkg._abi, pkg.workloads
     n = 64
-    prob = W.subset(W.config2(K=64, N=32), np.arange(n))
+    prob = W.subset(W.fourier_square(K=64, N=32), np.arange(n))
     tab = np.ascontiguousarray(engine.tabulate(prob, 3))
     assert tab.nbytes >= 1 << 20
     tprob = dict(prob)

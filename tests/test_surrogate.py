@@ -79,7 +79,7 @@ def test_training_reduces_loss_and_warm_start_saves_iterations(pkg, engine):
     hist = S.train(sur, feats, tgts, torch, epochs=4, batch=128, lr=1e-3)
     assert hist[-1] < 0.5 * hist[0]
     # warm-started solve on unseen cells: same answer, fewer iterations
-    prob = W.config2(K=16, N=32, seeds=(3, 30, 300))
+    prob = W.fourier_square(K=16, N=32, seeds=(3, 30, 300))
     desc, keep = S.device_problem(engine, prob, torch)
     cold = S.solve_device(engine, desc, torch, tol=1e-10)
     sur.attach()
@@ -121,7 +121,7 @@ def test_features_match_numpy(pkg, engine):
     device, so 1e-5 relative to the feature scale."""
     torch = pytest.importorskip("torch")
     S, W = pkg.surrogate, pkg.workloads
-    prob = W.subset(W.config2(K=64, N=32), [0, 5, 2047, 4095])
+    prob = W.subset(W.fourier_square(K=64, N=32), [0, 5, 2047, 4095])
     desc, keep = S.device_problem(engine, prob, torch)
     got = S.features(engine, desc, torch).cpu().numpy()
     tab = engine.tabulate(prob, 3).reshape(4, 3, 4, 32, 32)  # [cell][comp][q][cy][cx]

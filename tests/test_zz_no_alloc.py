@@ -83,7 +83,7 @@ def test_noalloc_tabulated_coefficient(pkg, engine):
     abi = pkg._abi
     lib = abi.load()
     W = pkg.workloads
-    prob = W.subset(W.config2(K=64, N=32), [0, 17, 300, 1999, 4095])
+    prob = W.subset(W.fourier_square(K=64, N=32), [0, 17, 300, 1999, 4095])
     tab = engine.tabulate(prob, 3)
     ref = engine.run(prob, precision="fp64", tol=1e-11, want_basis=True)
     corners_d = torch.from_numpy(prob["corners"]).cuda()
@@ -101,7 +101,7 @@ def test_noalloc_rejects_what_it_cannot_do(pkg):
     abi = pkg._abi
     lib = abi.load()
     W = pkg.workloads
-    prob = W.config1()
+    prob = W.sinsin_square()
     d = abi.BatchDesc()
     d.dim, d.n_fine, d.precision = 2, 16, abi.PREC_FP64
     corners = np.ascontiguousarray(prob["corners"])
