@@ -612,7 +612,7 @@ int msfem_create(msfem_handle **handle, int device) {
   MSFEM_CUDA(cudaGetDeviceProperties(&prop, device));
   if (prop.major != 10 || prop.minor != 3)
     return fail(MSFEM_ERR_NO_DEVICE, std::string("device is sm_") + std::to_string(prop.major) +
-                                         std::to_string(prop.minor) + ", this build targets sm_103a");
+                                         std::to_string(prop.minor) + ", the library is compiled for sm_103a");
   MSFEM_CUDA(cudaSetDevice(device));
   msfem_handle *h = new msfem_handle();
   h->device = device;
