@@ -98,7 +98,58 @@ int conv_tc_t(const ConvCtx &c, int B, const bf16 *X, const bf16 *W, const float
   return MSFEM_OK;
 }
 
+// Weight and bias gradient of one layer on the tcgen05 tensor cores: X
+// through the same kind of tensor map as the forward pass (the window rows of
+// 256-position items), G read directly.
+template <int XC, int GC>
+int wgrad_tc_t(const ConvCtx &c, int B, const bf16 *X, const bf16 *G, int cin_real, int cout_real, float *dW,
+               float *db, int dil, std::string *msg) {
+  if (B <= 0) return MSFEM_OK;
+  const EncodeTiledFn enc = tensor_map_encoder();
+  if (!enc) return fail(msg, MSFEM_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+  const tc::WgGeom g = tc::wg_geom(dil);
+  const cuuint64_t dims[3] = {2u * kW, (cuuint64_t)kH, (cuuint64_t)B * (XC / 8)};
+  const cuuint64_t strides[2] = {(cuuint64_t)kW * 16, (cuuint64_t)kPix * 16};
+  const cuuint32_t estr[3] = {1u, 1u, 1u};
+  const int rem = g.box_rows % tc::kBoxRows;
+  CUtensorMap maps[2];
+  for (int m = 0; m < 2; ++m) {
+    const cuuint32_t rows = m == 0 ? (cuuint32_t)tc::kBoxRows : (cuuint32_t)std::max(rem, 1);
+    const cuuint32_t box[3] = {2u * (cuuint32_t)g.wp, rows, 1u};
+    const CUresult r = enc(&maps[m], CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, const_cast<bf16 *>(X), dims, strides, box,
+                           estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS)
+      return fail(msg, MSFEM_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+  }
+  auto fn = tc::conv3x3_wgrad_tc_kernel<XC, GC>;
+  const size_t smem = tc::wgrad_tc_smem<XC>(dil);
+  CONV_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)tc::wgrad_tc_smem<XC>(kMaxDil)));
+  CONV_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                  (int)cudaSharedmemCarveoutMaxShared));
+  int smem_sm = 0, smem_rsv = 0;
+  CONV_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c.device));
+  CONV_CUDA(cudaDeviceGetAttribute(&smem_rsv, cudaDevAttrReservedSharedMemoryPerBlock, c.device));
+  int per_sm = smem_sm / (int)(smem + smem_rsv + 256);
+  per_sm = std::min(per_sm, (int)(512 / tc::wgrad_tmem_cols<XC>()));
+  if (per_sm < 1) return fail(msg, MSFEM_ERR_UNSUPPORTED, "tensor-core weight gradient does not fit on an SM");
+  const long items = (long)B * g.segs;
+  const int grid = (int)std::min<long>(items, (long)per_sm * c.sm_count);
+  fn<<<grid, tc::kWgThreads, smem, c.stream>>>(maps[0], maps[1], G, B, cin_real, cout_real, dW, db, dil, c.err);
+  CONV_CUDA(cudaGetLastError());
+  return MSFEM_OK;
+}
+
 }  // namespace
+
+int wgrad_tc(const ConvCtx &c, int xc, int gc, int B, const bf16 *X, const bf16 *G, int cin_real, int cout_real,
+             float *dW, float *db, int dil, std::string *msg) {
+  if (xc == 32 && gc == 16) return wgrad_tc_t<32, 16>(c, B, X, G, cin_real, cout_real, dW, db, dil, msg);
+  if (xc == 32 && gc == 32) return wgrad_tc_t<32, 32>(c, B, X, G, cin_real, cout_real, dW, db, dil, msg);
+  if (xc == 16 && gc == 32) return wgrad_tc_t<16, 32>(c, B, X, G, cin_real, cout_real, dW, db, dil, msg);
+  return fail(msg, MSFEM_ERR_UNSUPPORTED, "no compiled weight gradient for this layer kind");
+}
 
 int conv_tc(const ConvCtx &c, int cin, int cout, int epi, int B, const bf16 *X, const bf16 *W, const float *bias,
             const bf16 *mask, void *out, int cout_real, int dil, std::string *msg) {

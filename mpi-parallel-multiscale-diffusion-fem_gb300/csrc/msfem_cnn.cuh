@@ -13,8 +13,8 @@
 //            output = delta_i = phi_i - Q1_i at every node
 //   numerics BF16 weights and activations, FP32 accumulation on the tensor
 //            cores (tcgen05.mma kind::f16 with TMEM accumulators, in
-//            msfem_conv_tc.cuh); FP32 master weights and Adam; the weight
-//            gradient is an FP32 reduction on the CUDA cores.
+//            msfem_conv_tc.cuh) for the forward pass, the input gradient
+//            and the weight/bias gradient; FP32 master weights and Adam.
 //
 // Device layouts: activations channel-blocked BF16 [B][C/8][33][33][8] (8
 // channels = 16 bytes per pixel and block; C padded to 16 or 32: first layer
@@ -53,83 +53,8 @@ enum { EPI_RELU_BF16 = 0,   // out = bf16(relu(acc + b))          (hidden layers
        EPI_F32_NCHW = 1,    // out = float(acc + b), NCHW, real channels (last layer)
        EPI_MASK_BF16 = 2 }; // out = bf16(acc * [mask > 0])       (input gradient)
 
-// Weight/bias gradient of one layer, FP32 accumulation:
-//   dW[co][ci][tap] += sum_p G[p][co] X[p + tap][ci],  db[co] += sum_p G[p][co]
-// G: output gradient, GC channels; X: layer input, XC channels; both in the
-// channel-blocked layout [B][C/8][33][33][8] bf16.
-// Thread = (ci, 4 output channels); CTAs stride over the images.
-template <int XC, int GC>
-__global__ void __launch_bounds__(256)
-conv3x3_wgrad_kernel(const __nv_bfloat16 *__restrict__ X, const __nv_bfloat16 *__restrict__ G, int B,
-                     int cin_real, int cout_real, float *__restrict__ dW, float *__restrict__ db, int dil) {
-  const int HP = kH + 2 * dil;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  __nv_bfloat16 *s_x = reinterpret_cast<__nv_bfloat16 *>(smem_raw);   // [HP*HP][XC]
-  __nv_bfloat16 *s_g = s_x + HP * HP * XC;                              // [kPix][GC]
-  const int tid = threadIdx.x;
-  const int ngrp = (cout_real + 3) / 4;
-  const int ci = tid % 32, grp = tid / 32;  // 8 groups of 4 output channels
-  const bool act = ci < cin_real && grp < ngrp;
-  float acc[4][9], accb[4];
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    accb[j] = 0.f;
-#pragma unroll
-    for (int tp = 0; tp < 9; ++tp) acc[j][tp] = 0.f;
-  }
-  for (int b = blockIdx.x; b < B; b += gridDim.x) {
-    __syncthreads();
-    const __nv_bfloat16 *xb = X + (long)b * kPix * XC;  // blocked: [XC/8][33][33][8]
-    const __nv_bfloat16 *gb = G + (long)b * kPix * GC;
-    for (int i = tid; i < HP * HP * (XC / 8); i += 256) {
-      const int k = i / (HP * HP), pix = i % (HP * HP);
-      const int hy = pix / HP, hx = pix % HP;
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (hy >= dil && hy < kH + dil && hx >= dil && hx < kW + dil)
-        v = *reinterpret_cast<const uint4 *>(xb + ((long)k * kPix + (hy - dil) * kW + (hx - dil)) * 8);
-      *reinterpret_cast<uint4 *>(s_x + pix * XC + k * 8) = v;
-    }
-    for (int i = tid; i < kPix * (GC / 8); i += 256) {
-      const int k = i / kPix, pix = i % kPix;
-      *reinterpret_cast<uint4 *>(s_g + pix * GC + k * 8) =
-          *reinterpret_cast<const uint4 *>(gb + ((long)k * kPix + pix) * 8);
-    }
-    __syncthreads();
-    if (act) {
-      const int co0 = grp * 4;
-      for (int p = 0; p < kPix; ++p) {
-        const int y = p / kW, x = p % kW;
-        float gv[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) gv[j] = (co0 + j < cout_real) ? __bfloat162float(s_g[p * GC + co0 + j]) : 0.f;
-#pragma unroll
-        for (int tp = 0; tp < 9; ++tp) {
-          const float xv = __bfloat162float(s_x[((y + (tp / 3) * dil) * HP + x + (tp % 3) * dil) * XC + ci]);
-#pragma unroll
-          for (int j = 0; j < 4; ++j) acc[j][tp] = fmaf(gv[j], xv, acc[j][tp]);
-        }
-        if (ci == 0)
-#pragma unroll
-          for (int j = 0; j < 4; ++j) accb[j] += gv[j];
-      }
-    }
-  }
-  if (act) {
-    const int co0 = grp * 4;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      if (co0 + j >= cout_real) continue;
-#pragma unroll
-      for (int tp = 0; tp < 9; ++tp) atomicAdd(dW + ((long)(co0 + j) * cin_real + ci) * 9 + tp, acc[j][tp]);
-      if (ci == 0) atomicAdd(db + co0 + j, accb[j]);
-    }
-  }
-}
-
-template <int XC, int GC>
-constexpr size_t wgrad_smem(int dil) {
-  return sizeof(__nv_bfloat16) * ((size_t)(kH + 2 * dil) * (kW + 2 * dil) * XC + (size_t)kPix * GC);
-}
+// The weight/bias gradient runs on the tensor cores (conv3x3_wgrad_tc_kernel,
+// msfem_conv_tc.cuh).
 
 // Pack the FP32 parameters of layer l into the BF16 forward layout
 // [COUTp][9][CINp] and the transposed, tap-flipped layout [CINp][9][COUTp]

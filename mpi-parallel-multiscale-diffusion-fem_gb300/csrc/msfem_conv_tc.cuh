@@ -423,6 +423,209 @@ conv3x3_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constan
   if (warp == 0) tmem_dealloc(tbase, NCOL);
 }
 
+// ---------------------------------------------------------------------------
+// Weight and bias gradient on the tensor cores.
+//
+//   dW[cout][cin][tap] = sum_{b, p} G[b][p][cout] X[b][p + shift(tap)][cin],
+//   db[cout]           = sum_{b, p} G[b][p][cout],
+//
+// a GEMM per tap with K = the output positions of all images: D_tap(M x N)
+// += A(M x 16) B_tap(16 x N) per 16 positions, M = 128 rows of output
+// channels (GC real, the rest zero), N = XC input channels.  Both operands
+// are read MN-major straight from the channel-blocked layout (8 channels =
+// 16 contiguous bytes per position): B_tap is the TMA-loaded input window of
+// the forward pass (same tensor map geometry), the tap a shift of its start
+// address; A is the output gradient staged per 16 positions into 16 groups of
+// 8 channels, the groups beyond GC zero.  The bias gradient is one more
+// accumulator against a tile of ones.  Positions run over the forward pass's
+// padded-width grid, where G is zero outside the image, so every product of
+// the forward convolution appears exactly once.
+//
+// A CTA accumulates its items (image, 256 positions) in TMEM (9 + 1
+// accumulators of N columns) and adds them to dW/db with FP32 atomics at the
+// end.  Per item: TMA window + staged G -> one thread issues 16 x 10 MMAs ->
+// commit; every wait is bounded (err 1: window load, 2: MMA).
+// ---------------------------------------------------------------------------
+constexpr int kWgPos = 256;                              // positions (K) per item
+constexpr int kWgKsteps = kWgPos / 16;
+constexpr int kWgThreads = 256;
+constexpr uint32_t kWgKstepBytes = 16u * 256u;           // 16 channel groups x 16 positions x 16 B
+constexpr uint32_t kWgStaging = (uint32_t)kWgKsteps * kWgKstepBytes;  // 64 KB
+constexpr uint32_t kWgOnes = 1024u;                      // ones tile: up to 4 groups x 16 positions x 16 B
+
+struct WgGeom {
+  int dil, wp, npos, segs, box_rows;
+  uint32_t chunk_bytes, chunk_stride;
+};
+__host__ __device__ inline WgGeom wg_geom(int dil) {
+  WgGeom g;
+  g.dil = dil;
+  g.wp = kW + 2 * dil;
+  g.npos = kH * g.wp;
+  g.segs = (g.npos + kWgPos - 1) / kWgPos;
+  g.box_rows = (kWgPos + 2 * dil * g.wp + 2 * dil + g.wp - 1) / g.wp + 1;
+  g.chunk_bytes = (uint32_t)g.box_rows * g.wp * 16;
+  g.chunk_stride = (g.chunk_bytes + 1023u) & ~1023u;
+  return g;
+}
+template <int XC>
+__host__ inline size_t wgrad_tc_smem(int dil) {
+  return 1024 + kWgStaging + kWgOnes + (size_t)(XC / 8) * wg_geom(dil).chunk_stride;
+}
+template <int XC>
+__host__ __device__ constexpr uint32_t wgrad_tmem_cols() {
+  return 10 * XC <= 256 ? 256u : 512u;
+}
+
+template <int XC, int GC>
+__global__ void __launch_bounds__(kWgThreads, 1)
+conv3x3_wgrad_tc_kernel(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap xmap_rem,
+                        const __nv_bfloat16 *__restrict__ G, int B, int cin_real, int cout_real,
+                        float *__restrict__ dW, float *__restrict__ db, int dil, int *err) {
+  static_assert((XC == 16 || XC == 32) && (GC == 16 || GC == 32), "shapes");
+  constexpr int KC = XC / 8, GB = GC / 8;
+  constexpr uint32_t N = XC;
+  // A and B MN-major (bits 15, 16), M = 128, N = XC
+  constexpr uint32_t IDESC = idesc_bf16(128, N) | (1u << 15) | (1u << 16);
+  constexpr uint32_t NCOL = wgrad_tmem_cols<XC>();
+  extern __shared__ __align__(16) unsigned char smem_dyn[];
+  __shared__ __align__(8) uint64_t bar_tma, bar_mma;
+  __shared__ uint32_t tmem_base;
+  __shared__ int abort_code;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const WgGeom g = wg_geom(dil);
+  const uint32_t raw = smem_u32(smem_dyn);
+  const uint32_t s_stage = (raw + 1023u) & ~1023u;
+  const uint32_t s_ones = s_stage + kWgStaging;
+  const uint32_t s_x = s_ones + kWgOnes;
+  unsigned char *gen_stage = smem_dyn + (s_stage - raw);
+  unsigned char *gen_ones = gen_stage + kWgStaging;
+  // zero staging (its groups >= GC/8 stay zero: the padding rows of M = 128)
+  for (uint32_t i = tid; i < kWgStaging / 16; i += kWgThreads)
+    *reinterpret_cast<uint4 *>(gen_stage + 16 * i) = make_uint4(0, 0, 0, 0);
+  for (uint32_t i = tid; i < kWgOnes / 4; i += kWgThreads)
+    reinterpret_cast<uint32_t *>(gen_ones)[i] = 0x3F803F80u;  // bf16 1.0, 1.0
+  if (tid == 0) {
+    mbar_init(smem_u32(&bar_tma), 1);
+    mbar_init(smem_u32(&bar_mma), 1);
+    abort_code = 0;
+    fence_mbar_init();
+  }
+  if (warp == 0) tmem_alloc(smem_u32(&tmem_base), NCOL);
+  fence_proxy_async();
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  const uint32_t tbase = tmem_base;
+  uint32_t tap_off[9];
+#pragma unroll
+  for (int tap = 0; tap < 9; ++tap) tap_off[tap] = (uint32_t)((tap / 3) * dil * g.wp + (tap % 3) * dil);
+
+  const long items = (long)B * g.segs;
+  uint32_t phase = 0;
+  bool first = true;
+  bool tma_pending = false;
+  for (long it = blockIdx.x; it < items; it += gridDim.x) {
+    const int b = (int)(it / g.segs), seg = (int)(it % g.segs);
+    const int p0 = seg * kWgPos, r0 = p0 / g.wp;
+    if (tid == 0) {
+      // the input window, as in the forward pass: boxes of kBoxRows rows (128 wp
+      // bytes each, 128-byte aligned destinations) and the remainder
+      const uint32_t full = smem_u32(&bar_tma);
+      mbar_expect_tx(full, KC * g.chunk_bytes);
+      const int nfull = g.box_rows / kBoxRows, rem = g.box_rows - nfull * kBoxRows;
+      for (int k = 0; k < KC; ++k) {
+        const uint32_t dst = s_x + k * g.chunk_stride;
+        for (int q = 0; q < nfull; ++q)
+          tma_load_3d(dst + (uint32_t)(q * kBoxRows * g.wp * 16), &xmap, -2 * dil, r0 - dil + q * kBoxRows,
+                      b * KC + k, full);
+        if (rem > 0)
+          tma_load_3d(dst + (uint32_t)(nfull * kBoxRows * g.wp * 16), &xmap_rem, -2 * dil,
+                      r0 - dil + nfull * kBoxRows, b * KC + k, full);
+      }
+      tma_pending = true;
+    }
+    // the output gradient of the item's positions: [k-step][group][16 positions][8 ch]
+    for (int i = tid; i < kWgPos * GB; i += kWgThreads) {
+      const int grp = i / kWgPos, r = i - grp * kWgPos;
+      const int P = p0 + r, y = P / g.wp, x = P - y * g.wp;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (y < kH && x < kW)
+        v = *reinterpret_cast<const uint4 *>(G + (((long)b * GB + grp) * kPix + y * kW + x) * 8);
+      *reinterpret_cast<uint4 *>(gen_stage + (r >> 4) * kWgKstepBytes + grp * 256 + (r & 15) * 16) = v;
+    }
+    fence_proxy_async();  // generic-proxy staging stores -> tensor-core reads
+    __syncthreads();
+    if (tid == 0) {
+      if (!mbar_wait(smem_u32(&bar_tma), phase)) {
+        abort_code = 1;
+        atomicExch(err, 1);
+      } else {
+        tma_pending = false;
+        fence_after_sync();
+        const uint32_t pos0 = (uint32_t)(p0 - r0 * g.wp);  // item start within the window's first row
+        // MN-major operands: LBO = stride of the 8-row groups along K (the next
+        // 8 positions, 128 B), SBO = stride of the 8-channel groups along M/N
+        const uint64_t ones = smem_desc(s_ones, 128, 256);
+#pragma unroll 1
+        for (int ks = 0; ks < kWgKsteps; ++ks) {
+          const uint64_t a = smem_desc(s_stage + ks * kWgKstepBytes, 128, 256);
+          const uint32_t acc = (first && ks == 0) ? 0u : 1u;
+          const uint32_t xs = s_x + (pos0 + 16u * ks) * 16u;
+#pragma unroll
+          for (int tap = 0; tap < 9; ++tap)
+            umma_bf16(tbase + tap * N, a, smem_desc(xs + tap_off[tap] * 16u, 128, g.chunk_stride), IDESC, acc);
+          umma_bf16(tbase + 9 * N, a, ones, IDESC, acc);
+        }
+        umma_commit(smem_u32(&bar_mma));
+        if (!mbar_wait(smem_u32(&bar_mma), phase)) {
+          abort_code = 2;
+          atomicExch(err, 2);
+        }
+      }
+    }
+    __syncthreads();
+    if (abort_code) break;
+    phase ^= 1u;
+    first = false;
+  }
+  // a window copy still in flight must land before the CTA's smem goes, and
+  // MMAs still running before their TMEM is released
+  if (tid == 0 && tma_pending) mbar_wait(smem_u32(&bar_tma), phase);
+  if (tid == 0 && abort_code == 2) mbar_wait(smem_u32(&bar_mma), phase);
+  fence_after_sync();
+  if (!abort_code && !first && warp == 0) {
+    // rows (output channels) 0..31 sit in TMEM lanes 0..31: warp 0's quarter
+    const int co = threadIdx.x;
+    uint32_t v[32];
+#pragma unroll 1
+    for (int t = 0; t < 10; ++t) {
+      if constexpr (N == 32) {
+        tmem_ld32(tbase + t * N, v);
+      } else {
+        uint32_t h[16];
+        tmem_ld16(tbase + t * N, h);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] = h[j];
+      }
+      tmem_wait_ld();
+      if (co < cout_real) {
+        if (t < 9) {
+#pragma unroll
+          for (int ci = 0; ci < (int)N; ++ci)
+            if (ci < cin_real) atomicAdd(dW + ((long)co * cin_real + ci) * 9 + t, __uint_as_float(v[ci]));
+        } else {
+          atomicAdd(db + co, __uint_as_float(v[0]));
+        }
+      }
+    }
+  }
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  if (warp == 0) tmem_dealloc(tbase, NCOL);
+}
+
 }  // namespace tc
 }  // namespace cnn
 }  // namespace msfem

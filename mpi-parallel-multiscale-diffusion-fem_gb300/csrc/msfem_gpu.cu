@@ -846,16 +846,14 @@ int surrogate_check(msfem_surrogate *s) {
                                   (code == 1 ? "window loads (TMA)" : code == 2 ? "MMA issue" : "epilogue"));
 }
 
+// Weight and bias gradient of one layer on the tcgen05 tensor cores (cnn_tc.cu).
 template <int XC, int GC>
-int launch_wgrad(cudaStream_t st, int sms, int B, const bf16 *X, const bf16 *G, int cin_real, int cout_real,
-                 float *dW, float *db, int dil) {
-  const size_t smem = cn::wgrad_smem<XC, GC>(dil);
-  auto fn = cn::conv3x3_wgrad_kernel<XC, GC>;
-  MSFEM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)cn::wgrad_smem<XC, GC>(cn::kMaxDil)));
-  fn<<<std::max(1, std::min(B, sms)), 256, smem, st>>>(X, G, B, cin_real, cout_real, dW, db, dil);
-  MSFEM_CUDA(cudaGetLastError());
-  return MSFEM_OK;
+int launch_wgrad(msfem_surrogate *s, int B, const bf16 *X, const bf16 *G, int cin_real, int cout_real, float *dW,
+                 float *db, int dil) {
+  const cn::ConvCtx ctx{s->h->stream, s->h->device, s->h->sm_count, s->tc_err.as<int>()};
+  std::string msg;
+  const int rc = cn::wgrad_tc(ctx, XC, GC, B, X, G, cin_real, cout_real, dW, db, dil, &msg);
+  return rc ? fail(rc, msg) : MSFEM_OK;
 }
 
 int surrogate_reserve(msfem_surrogate *s, int B) {
@@ -917,23 +915,22 @@ int surrogate_backward(msfem_surrogate *s, const float *features, const float *t
       s->act[cn::kLayers].as<float>(), targets, B, scale, s->ga.as<bf16>(), s->loss.as<double>());
   MSFEM_CUDA(cudaGetLastError());
   float *G = s->grads.as<float>();
-  const int sms = s->h->sm_count;
   auto dW = [&](int l) { return G + cn::param_offset(l); };
   auto db = [&](int l) { return G + cn::param_offset(l) + (long)cn::real_ch(l + 1) * cn::real_ch(l) * 9; };
   // layer 6: g (16 ch) in ga
-  if ((rc = launch_wgrad<32, 16>(st, sms, B, s->act[5].as<bf16>(), s->ga.as<bf16>(), 32, 4, dW(5), db(5),
+  if ((rc = launch_wgrad<32, 16>(s, B, s->act[5].as<bf16>(), s->ga.as<bf16>(), 32, 4, dW(5), db(5),
                                  cn::dilation(5)))) return rc;
   if ((rc = launch_conv<16, 32, cn::EPI_MASK_BF16>(s, B, s->ga.as<bf16>(), s->wt[5].as<bf16>(), nullptr,
                                                   s->act[5].as<bf16>(), s->gb.ptr, 32, cn::dilation(5)))) return rc;
   bf16 *g = s->gb.as<bf16>(), *gn = s->ga.as<bf16>();
   for (int l = 4; l >= 1; --l) {
-    if ((rc = launch_wgrad<32, 32>(st, sms, B, s->act[l].as<bf16>(), g, 32, 32, dW(l), db(l), cn::dilation(l))))
+    if ((rc = launch_wgrad<32, 32>(s, B, s->act[l].as<bf16>(), g, 32, 32, dW(l), db(l), cn::dilation(l))))
       return rc;
     if ((rc = launch_conv<32, 32, cn::EPI_MASK_BF16>(s, B, g, s->wt[l].as<bf16>(), nullptr, s->act[l].as<bf16>(),
                                                     gn, 32, cn::dilation(l)))) return rc;
     std::swap(g, gn);
   }
-  return launch_wgrad<16, 32>(st, sms, B, s->act[0].as<bf16>(), g, 3, 32, dW(0), db(0), cn::dilation(0));
+  return launch_wgrad<16, 32>(s, B, s->act[0].as<bf16>(), g, 3, 32, dW(0), db(0), cn::dilation(0));
 }
 
 // The warm start inside msfem_run_batch: features -> prediction -> Q1 + delta.

@@ -50,6 +50,11 @@ struct ConvCtx {
 // msfem_status code; *msg says why on failure.
 int conv_tc(const ConvCtx &c, int cin, int cout, int epi, int B, const __nv_bfloat16 *X, const __nv_bfloat16 *W,
             const float *bias, const __nv_bfloat16 *mask, void *out, int cout_real, int dil, std::string *msg);
+// Weight and bias gradient of one layer on the tcgen05 tensor cores (cnn_tc.cu):
+// dW [cout_real][cin_real][9] and db [cout_real] (FP32) are accumulated into
+// with atomics; (xc, gc) the padded channel counts of X and G.
+int wgrad_tc(const ConvCtx &c, int xc, int gc, int B, const __nv_bfloat16 *X, const __nv_bfloat16 *G, int cin_real,
+             int cout_real, float *dW, float *db, int dil, std::string *msg);
 }  // namespace cnn
 
 }  // namespace msfem
