@@ -720,8 +720,8 @@ def main():
         ev["mixed_surrogate"]["speedup_vs_fp64_cold"] = ev["fp64_cold"]["ms"] / ev["mixed_surrogate"]["ms"]
         line["surrogate"] = {
             "network": "6 conv3x3 layers 3-32-32-32-32-32-4, dilations 1/2/4/8/2/1, BF16 weights and "
-                       "activations, FP32 accumulation (tcgen05.mma kind::f16, TMEM accumulators, TMA-staged windows), "
-                       "Adam lr 1e-3",
+                       "activations, FP32 accumulation (tcgen05.mma kind::f16, TMEM accumulators, TMA-staged windows) "
+                       "for the forward pass, the input gradient and the weight/bias gradient; Adam lr 1e-3",
             "training": {"solves": int(4 * 12 * 4096), "epochs": 20, "batch": 256,
                          "data_seconds": t_data, "train_seconds": t_train,
                          "loss_first_epoch": hist[0], "loss_last_epoch": hist[-1]},
