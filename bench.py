@@ -342,9 +342,9 @@ def main():
         """Energy-norm error of every basis function (msfem_energy_error) and
         the coarse-matrix error of every cell, got against ref."""
         d = desc if desc is not None else device_desc(ws, abi.PREC_FP64)
-        n = d.n_cells
-        err = torch.empty((n, 4), dtype=torch.float64, device=f"cuda:{local}")
-        nrm = torch.empty((n, 4), dtype=torch.float64, device=f"cuda:{local}")
+        n, nv = d.n_cells, 1 << d.dim
+        err = torch.empty((n, nv), dtype=torch.float64, device=f"cuda:{local}")
+        nrm = torch.empty((n, nv), dtype=torch.float64, device=f"cuda:{local}")
         rc = eng.lib.msfem_energy_error(eng.handle, ctypes.byref(d), got["basis"].data_ptr(),
                                         ref["basis"].data_ptr(), err.data_ptr(), nrm.data_ptr())
         if rc != abi.OK:
@@ -666,6 +666,29 @@ def main():
             res4[pname]["cg_frac_of_measured_" + ("fp64" if prec == abi.PREC_FP64 else "fp32") + "_peak"] = \
                 flw / (ms * 1e-3) / peak
         res4["speedup_mixed_vs_fp64"] = res4["fp64"]["ms_per_step"] / res4["mixed"]["ms_per_step"]
+        # per-basis energy errors and coarse-matrix errors of both forms
+        # against the FP64 form solved to 1e-12 (untimed)
+        bsz4 = int(np.sum(8 * (nf4_h.astype(np.int64) + 1) ** 3))
+
+        def solve4(precision, tol):
+            d = desc4(precision)
+            d.tol = tol
+            out = {"M": torch.empty((nc4, 8, 8), dtype=torch.float64, device=f"cuda:{local}"),
+                   "F": torch.empty((nc4, 8), dtype=torch.float64, device=f"cuda:{local}"),
+                   "basis": torch.empty(bsz4, dtype=torch.float64, device=f"cuda:{local}")}
+            _, out["stats"] = eng.run_desc(d, out["M"].data_ptr(), out["F"].data_ptr(), out["basis"].data_ptr(),
+                                           st4.data_ptr(), it4.data_ptr(), stats=True)
+            return out
+
+        ref4 = solve4(abi.PREC_FP64, 1e-12)
+        res4["errors_reference"] = ("FP64 form solved to 1e-12 relative residual (max "
+                                    f"{ref4['stats']['max_rel_residual']:.2e}); energy norm ||phi - phi_ref||_A / "
+                                    "||phi_ref||_A per basis function, |M_ij - M_ref,ij| / max |M_ref| per cell")
+        for prec, pname in ((abi.PREC_FP64, "fp64"), (abi.PREC_MIXED, "mixed")):
+            got4 = solve4(prec, TOL)
+            res4[pname]["errors_vs_fp64_1e-12"] = basis_errors(None, got4, ref4, desc=desc4(abi.PREC_FP64))
+            del got4
+        del ref4
         line["spheres_3d"] = res4
         del tab4, M4, F4, st4, it4, corners4, nf4
         torch.cuda.empty_cache()
