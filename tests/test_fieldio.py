@@ -64,3 +64,22 @@ def test_loaded_field_on_the_gpu(pkg, oracle, engine, tmp_path):
     ref = oracle.run(pkg.fieldio.load_field(path))
     assert got["rc"] == 0
     assert np.abs(got["M"] - ref["M"]).max() < 1e-10 * np.abs(ref["M"]).max()
+
+
+def test_round_trip_3d_scalar(pkg, oracle, tmp_path):
+    """A 3D uneven-N scalar field (the sphere workload's layout, ncomp = 1)."""
+    W, F = pkg.workloads, pkg.fieldio
+    rng = np.random.default_rng(3)
+    sp = np.column_stack([rng.uniform(0, 1, (50, 3)), rng.uniform(0.05, 0.1, 50)])
+    prob = W.problem(3, W.unit_cube_corners(3, 2)[:3], np.array([2, 4, 3], dtype=np.int32),
+                     {"kind": 4, "params": [1e4], "spheres": sp})
+    tab = oracle.tabulate(prob, 1)
+    path = tmp_path / "f3.msfield"
+    F.save_field(path, prob, tab, 1)
+    got = F.load_field(path, mmap=False)
+    assert got["dim"] == 3 and got["coef"]["ncomp"] == 1
+    assert np.array_equal(got["coef"]["qp_values"], tab)
+    assert np.array_equal(got["n_fine_per_cell"], prob["n_fine_per_cell"])
+    a = oracle.run(dict(prob, coef={"kind": pkg._abi.COEF_TABULATED, "ncomp": 1, "qp_values": tab}))
+    b = oracle.run(got)
+    assert np.array_equal(a["M"], b["M"])
