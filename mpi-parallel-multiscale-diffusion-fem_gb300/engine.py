@@ -43,9 +43,12 @@ class Engine:
             pass
 
     def set_stream(self, stream_handle):
+        """Launch on the caller's CUDA stream (0 / None: the handle's own
+        non-blocking stream)."""
         rc = self.lib.msfem_set_stream(self.handle, ctypes.c_void_p(stream_handle or 0))
         if rc != _abi.OK:
             raise _abi.MsfemError(rc, _abi.last_error(self.lib))
+        self.stream_handle = stream_handle or 0
 
     # -- descriptor -------------------------------------------------------
     @staticmethod

@@ -58,11 +58,15 @@ class Surrogate:
                                                        feats.shape[0], g.ctypes.data, ctypes.byref(loss)))
         return loss.value, g
 
-    def train_step(self, feats, targets, lr):
+    def train_step(self, feats, targets, lr, want_loss=True):
+        """One Adam step; returns the batch loss, or None without want_loss
+        (no device synchronisation: the step's launches queue behind the
+        previous ones)."""
         loss = ctypes.c_double()
         self._check(self.lib.msfem_surrogate_train_step(self.handle, feats.data_ptr(), targets.data_ptr(),
-                                                        feats.shape[0], lr, ctypes.byref(loss)))
-        return loss.value
+                                                        feats.shape[0], lr,
+                                                        ctypes.byref(loss) if want_loss else None))
+        return loss.value if want_loss else None
 
     def attach(self):
         self._check(self.lib.msfem_attach_surrogate(self.engine.handle, self.handle))
@@ -160,22 +164,43 @@ def training_set(engine, torch, seeds=None, K=64, log=None):
     return torch.cat(feats), torch.cat(tgts)
 
 
-def train(sur, feats, targets, torch, epochs=20, batch=256, lr=1e-3, seed=0, log=None):
-    """Adam with a fixed learning rate over shuffled mini-batches."""
+def train(sur, feats, targets, torch, epochs=20, batch=256, lr=1e-3, seed=0, log=None, loss_every=1):
+    """Adam with a fixed learning rate over shuffled mini-batches.  The batch
+    loss is read back (a device synchronisation) every `loss_every` steps and
+    at the last step of each epoch; an epoch's history entry is the mean of
+    the losses read in it (every step's by default)."""
     n = feats.shape[0]
     gen = torch.Generator(device="cuda")
     gen.manual_seed(seed)
+    steps = max(1, (n - batch) // batch + 1) if n >= batch else 0
+    # the mini-batch gathers run on torch's stream and the steps must follow
+    # them (and torch may reuse a batch's memory only after its step): the
+    # library launches on torch's current stream while training
+    engine = sur.engine
+    prev = getattr(engine, "stream_handle", 0)
+    engine.set_stream(torch.cuda.current_stream().cuda_stream)
+    try:
+        history = _train_epochs(sur, feats, targets, torch, epochs, batch, lr, gen, n, steps, loss_every, log)
+    finally:
+        engine.set_stream(prev)
+    return history
+
+
+def _train_epochs(sur, feats, targets, torch, epochs, batch, lr, gen, n, steps, loss_every, log):
     history = []
     t0 = time.time()
     for ep in range(epochs):
         perm = torch.randperm(n, device="cuda", generator=gen)
         tot, cnt = 0.0, 0
-        for b0 in range(0, n - batch + 1, batch):
+        for k, b0 in enumerate(range(0, n - batch + 1, batch)):
             idx = perm[b0:b0 + batch]
             fb = feats.index_select(0, idx).contiguous()
             tb = targets.index_select(0, idx).contiguous()
-            tot += sur.train_step(fb, tb, lr)
-            cnt += 1
+            read = (k % loss_every == loss_every - 1) or k == steps - 1
+            loss = sur.train_step(fb, tb, lr, want_loss=read)
+            if read:
+                tot += loss
+                cnt += 1
         history.append(tot / max(1, cnt))
         if log:
             log(f"epoch {ep + 1}: loss {history[-1]:.3e} ({time.time() - t0:.1f} s)")
