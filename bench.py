@@ -54,8 +54,8 @@ def dist_env():
 
 
 def flops_per_solve_iter(N):
-    """SURVEY-style algorithmic work of one CG iteration of one solve (2D):
-    2 nnz(A_II) + 11 n_I, nnz(A_II) = (3N-5)^2, n_I = (N-1)^2."""
+    """Algorithmic work of one CG iteration of one 2D solve: 2 nnz(A_II) +
+    11 n_I, nnz(A_II) = (3N-5)^2, n_I = (N-1)^2."""
     return 2 * (3 * N - 5) ** 2 + 11 * (N - 1) ** 2
 
 

@@ -188,6 +188,14 @@ int msfem_destroy(msfem_handle *handle);
  * pass cudaStreamLegacy. */
 int msfem_set_stream(msfem_handle *handle, void *cuda_stream);
 
+/* CUDA-graph use of the handle: how many graphs msfem_run_batch has captured
+ * and how many graph launches it has made.  Device-resident calls without
+ * stats (desc->memory == MSFEM_MEM_DEVICE, stats == NULL) on a stream other
+ * than the legacy default stream replay one graph of the queue reset and the
+ * basis kernel; a change of pointers, sizes or tuning re-captures it.  No
+ * counterpart in the reference (diagnostics of the batching layer). */
+int msfem_graph_info(msfem_handle *handle, int64_t *captures, int64_t *replays);
+
 /* Compute the multiscale basis of a batch of coarse cells.
  *   M            [n_cells][2^d][2^d]   coarse element matrices
  *   F            [n_cells][2^d]        coarse element loads
@@ -284,11 +292,12 @@ int64_t msfem_tabulated_size(const msfem_batch_desc *desc, int32_t ncomp);
 #define MSFEM_NOALLOC_MAX_CELLS 65536
 
 /* No counterpart in the reference: an entry point for callers that cannot
- * allocate device memory.  cudaMalloc synchronises the whole device and is
- * illegal while a stream is being captured, so a caller running inside its own
- * captured graph, inside a latency-critical time loop, or under a framework
- * that owns every device allocation (a fixed memory budget or pool) cannot use
- * msfem_run_batch, whose first call sizes device buffers on demand.
+ * allocate device memory.  msfem_run_batch sizes its device buffers on demand
+ * (cudaMalloc on the first call, and again whenever a batch outgrows them).
+ * Some callers cannot allow that: a framework that owns every device
+ * allocation of the process (a fixed memory budget or pool, where a hidden
+ * cudaMalloc either fails or breaks the accounting), or a latency-critical
+ * time loop, where cudaMalloc/cudaFree synchronise the whole device.
  *
  * This variant of the 2D basis kernel allocates nothing: no cudaMalloc, no
  * cudaFree, no handle, no allocating library call.  Its scratch (the
@@ -299,10 +308,14 @@ int64_t msfem_tabulated_size(const msfem_batch_desc *desc, int32_t ncomp);
  *     MSFEM_MEM_DEVICE: every pointer in desc and every output is a device
  *     pointer the caller owns.  Coefficient kinds CONSTANT, REFERENCE, SINSIN
  *     and TABULATED (FOURIER/SPHERES need a tabulation buffer: tabulate first).
+ *     Warm starts NONE and USER; MSFEM_WARM_SURROGATE is rejected
+ *     (MSFEM_ERR_UNSUPPORTED): the network lives in a handle.
  *   - n_cells above MSFEM_NOALLOC_MAX_CELLS is rejected (MSFEM_ERR_INVALID_ARG).
+ *   - It always runs the default compiled launch shape with the default
+ *     parameters (residual-check interval, inner FP32 reduction): there is no
+ *     handle, so msfem_autotune / msfem_set_tuning choices do not apply.
  *   - The first call on a device looks up the scratch array's device address
- *     (with that device current); make that first call before any stream
- *     capture begins.
+ *     (with that device current).
  *   - The call only enqueues work on `stream` (a cudaStream_t, NULL = legacy
  *     default stream) and returns; outputs are valid once the stream has
  *     completed, and per-cell failures are reported in cell_status only.
@@ -310,7 +323,8 @@ int64_t msfem_tabulated_size(const msfem_batch_desc *desc, int32_t ncomp);
  *     contents; the counter is cleared on `stream` before each launch.  Calls
  *     that may overlap on the GPU (different streams without ordering) race on
  *     it: serialise them.
- * Results equal msfem_run_batch's on the same inputs. */
+ * Results equal msfem_run_batch's on the same inputs with the default launch
+ * choice. */
 int msfem_run_batch_noalloc(const msfem_batch_desc *desc, double *M, double *F,
                             double *basis, int32_t *cell_status,
                             int32_t *iterations, void *stream);

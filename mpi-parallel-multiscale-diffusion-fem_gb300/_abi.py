@@ -42,6 +42,10 @@ WARM_NONE = 0
 WARM_USER = 1
 WARM_SURROGATE = 2
 
+# cudaStreamLegacy: the legacy default stream (a NULL stream selects the
+# handle's own non-blocking stream in msfem_set_stream)
+CUDA_STREAM_LEGACY = 1
+
 MAX_N_2D = 32
 MAX_N_3D = 24
 NOALLOC_MAX_CELLS = 65536
@@ -132,6 +136,8 @@ EXPORTS = {
     "msfem_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int]),
     "msfem_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "msfem_set_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "msfem_graph_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64),
+                                        ctypes.POINTER(ctypes.c_int64)]),
     "msfem_run_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BatchDesc),
                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_void_p, ctypes.c_void_p,

@@ -89,6 +89,7 @@ struct msfem_handle {
   std::string graph_key;
   cudaGraphExec_t graph_exec = nullptr;
   int64_t graph_launches = 0;
+  int64_t graph_captures = 0;
   // autotuned launch choices, keyed by (dim, N class, precision)
   std::map<int, Tune> tuning;
 };
@@ -535,12 +536,17 @@ int msfem_run_batch_noalloc(const msfem_batch_desc *d, double *M, double *F, dou
   if (kind != MSFEM_COEF_CONSTANT && kind != MSFEM_COEF_REFERENCE && kind != MSFEM_COEF_SINSIN &&
       kind != MSFEM_COEF_TABULATED)
     return fail(MSFEM_ERR_UNSUPPORTED, "msfem_run_batch_noalloc: tabulate FOURIER/SPHERES coefficients first");
+  if (d->warm_start == MSFEM_WARM_SURROGATE)
+    return fail(MSFEM_ERR_UNSUPPORTED,
+                "msfem_run_batch_noalloc: MSFEM_WARM_SURROGATE needs a handle and its buffers; use msfem_run_batch");
   if (d->n_cells > 0 && (!M || !F || !cell_status))
     return fail(MSFEM_ERR_INVALID_ARG, "msfem_run_batch_noalloc: M, F and cell_status are required");
   if (d->n_cells == 0) return MSFEM_OK;
   const bool mixed = d->precision == MSFEM_PREC_MIXED;
   const std::vector<Launch> cands = candidates(2, d->n_fine, mixed);
   if (cands.empty()) return fail(MSFEM_ERR_UNSUPPORTED, "no kernel for this N");
+  // the default compiled shape and parameters: this entry has no handle, so
+  // no autotuned choice applies
   const Launch L = cands[0];
   int device = 0;
   MSFEM_CUDA(cudaGetDevice(&device));
@@ -641,6 +647,13 @@ int msfem_destroy(msfem_handle *h) {
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   delete h;
+  return MSFEM_OK;
+}
+
+int msfem_graph_info(msfem_handle *h, int64_t *captures, int64_t *replays) {
+  if (!h) return fail(MSFEM_ERR_INVALID_ARG, "handle is NULL");
+  if (captures) *captures = h->graph_captures;
+  if (replays) *replays = h->graph_launches;
   return MSFEM_OK;
 }
 
@@ -1401,6 +1414,7 @@ int run_batch_impl(msfem_handle *h, const msfem_batch_desc *d, double *M, double
         return fail(MSFEM_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e4));
       }
       h->graph_key = key;
+      h->graph_captures++;
     }
     MSFEM_CUDA(cudaGraphLaunch(h->graph_exec, h->stream));
     launches++;

@@ -50,6 +50,14 @@ class Engine:
             raise _abi.MsfemError(rc, _abi.last_error(self.lib))
         self.stream_handle = stream_handle or 0
 
+    def graph_info(self):
+        """(captures, replays) of the handle's CUDA graph (msfem_graph_info)."""
+        c, r = ctypes.c_int64(0), ctypes.c_int64(0)
+        rc = self.lib.msfem_graph_info(self.handle, ctypes.byref(c), ctypes.byref(r))
+        if rc != _abi.OK:
+            raise _abi.MsfemError(rc, _abi.last_error(self.lib))
+        return c.value, r.value
+
     # -- descriptor -------------------------------------------------------
     @staticmethod
     def make_desc(problem, precision="fp64", tol=1e-10, maxit=1000, check_interval=0,

@@ -164,6 +164,15 @@ def training_set(engine, torch, seeds=None, K=64, log=None):
     return torch.cat(feats), torch.cat(tgts)
 
 
+def library_stream(torch):
+    """cudaStream_t handle of torch's current stream, for msfem_set_stream.
+    torch reports its legacy default stream as 0, and a NULL stream would put
+    the library on the handle's own non-blocking stream, which does not wait
+    for work on the legacy stream: map 0 to cudaStreamLegacy."""
+    h = torch.cuda.current_stream().cuda_stream
+    return h if h else _abi.CUDA_STREAM_LEGACY
+
+
 def train(sur, feats, targets, torch, epochs=20, batch=256, lr=1e-3, seed=0, log=None, loss_every=1):
     """Adam with a fixed learning rate over shuffled mini-batches.  The batch
     loss is read back (a device synchronisation) every `loss_every` steps and
@@ -178,7 +187,7 @@ def train(sur, feats, targets, torch, epochs=20, batch=256, lr=1e-3, seed=0, log
     # library launches on torch's current stream while training
     engine = sur.engine
     prev = getattr(engine, "stream_handle", 0)
-    engine.set_stream(torch.cuda.current_stream().cuda_stream)
+    engine.set_stream(library_stream(torch))
     try:
         history = _train_epochs(sur, feats, targets, torch, epochs, batch, lr, gen, n, steps, loss_every, log)
     finally:

@@ -57,8 +57,37 @@ def test_sphere_cells_against_oracle(pkg, oracle, engine, sphere_field, precisio
     got = engine.run(prob, precision=precision, tol=1e-12)
     ref = oracle.run(prob)
     assert got["rc"] == 0 and np.all(got["status"] == 0)
-    assert rel_err(got["M"], ref["M"]) < 1e-9
+    assert rel_err(got["M"], ref["M"]) < 1e-10
     assert rel_err(got["F"], ref["F"]) < 1e-10
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_every_compiled_3d_shape_at_sphere_field_sizes(pkg, oracle, engine, sphere_field, precision):
+    """Every compiled 3D launch shape the autotuner can pick -- one CTA per
+    cell at each register cap, and the 8-CTA thread-block cluster per cell --
+    on cells of the full sphere field with N = 24, 16 and 8 (the z-pair
+    stencil instantiations) in one uneven-N launch, against the oracle."""
+    W = pkg.workloads
+    nf = sphere_field["n_fine_per_cell"]
+    cells = [int(np.flatnonzero(nf == v)[1]) for v in (24, 16, 8)]
+    prob = W.subset(sphere_field, cells)
+    ref = oracle.run(prob, want_basis=True)
+    prec = 0 if precision == "fp64" else 1
+    probe = engine.autotune(prob, precision=precision, tol=1e-12, sample_cells=3)
+    assert probe["n_variants"] >= 2
+    try:
+        for v in range(probe["n_variants"]):
+            engine.set_tuning({"dim": 3, "n_max": 24, "precision": prec, "variant": v, "check_interval": 0,
+                               "inner_tol": 1e-6})
+            got = engine.run(prob, precision=precision, tol=1e-12, want_basis=True)
+            assert got["rc"] == 0 and np.all(got["status"] == 0), v
+            assert got["stats"]["kernel_launches"] == 2, v  # tabulation + one basis kernel
+            assert rel_err(got["M"], ref["M"]) < 1e-10, (v, rel_err(got["M"], ref["M"]))
+            assert rel_err(got["F"], ref["F"]) < 1e-10, (v, rel_err(got["F"], ref["F"]))
+            assert np.abs(got["basis"] - ref["basis"]).max() < 1e-9, v
+    finally:
+        engine.set_tuning({"dim": 3, "n_max": 24, "precision": prec, "variant": 0, "check_interval": 0,
+                           "inner_tol": 1e-6})
 
 
 def test_fourier_64_full_batch_invariants(pkg, engine):
@@ -68,7 +97,7 @@ def test_fourier_64_full_batch_invariants(pkg, engine):
     check_invariants(got["M"], got["F"], 1.0, 1e-9, 1e-9)  # f = 1 on the unit square
     mixed = engine.run(prob, precision="mixed", tol=1e-10)
     assert mixed["rc"] == 0
-    assert rel_err(mixed["M"], got["M"]) < 1e-9
+    assert rel_err(mixed["M"], got["M"]) < 1e-10
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])

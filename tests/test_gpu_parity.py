@@ -167,7 +167,7 @@ def test_mixed_reaches_tolerance_and_matches_fp64(pkg, engine):
     b = engine.run(prob, precision="mixed", tol=1e-10)
     assert a["stats"]["max_rel_residual"] < 1e-10
     assert b["stats"]["max_rel_residual"] < 1e-10
-    assert rel_err(b["M"], a["M"]) < 1e-9
+    assert rel_err(b["M"], a["M"]) < 1e-10
 
 
 @pytest.mark.parametrize("n_max", [32, 16])

@@ -68,9 +68,9 @@ def test_spheres_uneven_one_launch(pkg, oracle, engine, precision):
     ref = oracle.run(prob, want_basis=True)
     assert got["stats"]["kernel_launches"] == 2  # tabulation + one basis kernel
     assert got["rc"] == 0 and np.all(got["status"] == 0)
-    assert rel_err(got["M"], ref["M"]) < 1e-9
+    assert rel_err(got["M"], ref["M"]) < TOL_REL
     assert rel_err(got["F"], ref["F"]) < TOL_REL
-    assert np.abs(got["basis"] - ref["basis"]).max() < 1e-8
+    assert np.abs(got["basis"] - ref["basis"]).max() < 1e-9
 
 
 def test_fp64_iterations_match_oracle_jacobi_pcg_3d(pkg, oracle, engine):
@@ -100,7 +100,8 @@ def test_every_compiled_launch_shape_gives_the_same_answer_3d(pkg, oracle, engin
                            "inner_tol": 1e-6})
         got = engine.run(prob, precision=precision, tol=1e-12, want_basis=True)
         assert got["rc"] == 0 and np.all(got["status"] == 0), v
-        assert rel_err(got["M"], ref["M"]) < 1e-9, v
-        assert np.abs(got["basis"] - ref["basis"]).max() < 1e-8, v
+        assert rel_err(got["M"], ref["M"]) < TOL_REL, v
+        assert rel_err(got["F"], ref["F"]) < TOL_REL, v
+        assert np.abs(got["basis"] - ref["basis"]).max() < 1e-9, v
     engine.set_tuning({"dim": 3, "n_max": 9, "precision": prec, "variant": 0, "check_interval": 0,
                        "inner_tol": 1e-6})

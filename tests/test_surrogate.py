@@ -1,6 +1,8 @@
 """The learned warm start: the GPU forward/backward kernels against the numpy
 FP64 oracle (which itself is checked against finite differences), training,
 and the warm-started solve keeping parity with the cold one."""
+import types
+
 import numpy as np
 import pytest
 
@@ -22,6 +24,32 @@ def test_oracle_backward_matches_finite_differences(oracle):
         lm, _ = co.loss_and_grads(params - e, feats, tgts, bf16_mode=False)
         fd = (lp - lm) / 2e-5
         assert abs(fd - g[i]) <= 1e-6 + 1e-4 * abs(fd), (i, fd, g[i])
+
+
+def _fake_torch(current_stream_handle):
+    """The few torch calls train() makes before its first step."""
+    gen = types.SimpleNamespace(manual_seed=lambda seed: None)
+    cuda = types.SimpleNamespace(
+        current_stream=lambda: types.SimpleNamespace(cuda_stream=current_stream_handle))
+    return types.SimpleNamespace(cuda=cuda, Generator=lambda device=None: gen)
+
+
+@pytest.mark.parametrize("torch_stream, library_stream", [(0, 1), (0x5a5a00, 0x5a5a00)])
+def test_training_runs_on_torchs_stream(pkg, torch_stream, library_stream):
+    """train() points the library at torch's current stream for the training
+    steps (the mini-batch gathers run there) and restores the previous stream.
+    torch's legacy default stream (handle 0) must become cudaStreamLegacy (1):
+    a NULL stream would leave the library on its own non-blocking stream, which
+    does not wait for the gathers."""
+    S = pkg.surrogate
+    calls = []
+    engine = types.SimpleNamespace(stream_handle=0, set_stream=calls.append)
+    sur = types.SimpleNamespace(engine=engine)
+    feats = types.SimpleNamespace(shape=(512, 3, 33, 33))
+    hist = S.train(sur, feats, None, _fake_torch(torch_stream), epochs=0)
+    assert hist == []
+    assert calls == [library_stream, 0]
+    assert pkg._abi.CUDA_STREAM_LEGACY == 1
 
 
 def test_param_count_matches_library(built):
@@ -88,7 +116,7 @@ def test_training_reduces_loss_and_warm_start_saves_iterations(pkg, engine):
     assert warm["stats"]["cells_failed"] == 0
     assert warm["stats"]["max_rel_residual"] < 1e-10
     Mc, Mw = cold["M"].cpu().numpy(), warm["M"].cpu().numpy()
-    assert np.abs(Mc - Mw).max() < 1e-9 * np.abs(Mc).max()
+    assert np.abs(Mc - Mw).max() < 1e-10 * np.abs(Mc).max()
     assert warm["stats"]["iterations_total"] < cold["stats"]["iterations_total"]
     sur.close()
 

@@ -1,9 +1,11 @@
 """msfem_run_batch_noalloc: the entry point for callers that cannot allocate
-device memory (code inside their own stream capture, latency-critical loops,
-or frameworks that own every device allocation -- cudaMalloc synchronises the
-device and is illegal during capture).  It must give the same coarse matrices,
-loads and basis as msfem_run_batch, call after call, while using only the
-library's fixed scratch array.  Collected last on purpose (file name)."""
+device memory -- frameworks that own every device allocation of the process
+(a fixed pool or budget, where a hidden cudaMalloc fails or breaks the
+accounting) and latency-critical time loops (cudaMalloc and cudaFree
+synchronise the whole device).  It must give the same coarse matrices, loads
+and basis as msfem_run_batch, and as the oracle's direct solve, call after
+call, while using only the library's fixed scratch array.  Collected last on
+purpose (file name)."""
 import ctypes
 
 import numpy as np
@@ -54,13 +56,14 @@ def run_noalloc(torch, lib, abi, d, n, n_nodes):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_noalloc_matches_run_batch_twice(pkg, engine, precision):
+def test_noalloc_matches_run_batch_twice(pkg, oracle, engine, precision):
     torch = pytest.importorskip("torch")
     abi = pkg._abi
     lib = abi.load()
     prob = pkg.workloads.reference_problem(2, 3, 4)  # MatrixCoeff, f = 2, 64 cells, N = 16
     ref = engine.run(prob, precision=precision, tol=1e-12, want_basis=True)
     assert ref["rc"] == abi.OK
+    direct = oracle.run(prob, want_basis=True)  # the oracle's banded-Cholesky solve
     n, n_nodes = prob["corners"].shape[0], 17 * 17
     corners_d = torch.from_numpy(prob["corners"]).cuda()
     prec = abi.PREC_FP64 if precision == "fp64" else abi.PREC_MIXED
@@ -72,9 +75,39 @@ def test_noalloc_matches_run_batch_twice(pkg, engine, precision):
         assert rel_err(M, ref["M"]) < TOL_REL
         assert rel_err(F, ref["F"]) < TOL_REL
         assert np.abs(B - ref["basis"]).max() < 1e-9
+        assert rel_err(M, direct["M"]) < TOL_REL
+        assert rel_err(F, direct["F"]) < TOL_REL
+        assert np.abs(B - direct["basis"]).max() < 1e-9
         if first is not None:
             assert np.array_equal(M, first)
         first = M
+
+
+def test_noalloc_allocates_nothing(pkg, engine):
+    """After the first call on the device (which loads the kernel and looks up
+    the scratch address), further calls change neither torch's allocator nor
+    the device's free memory."""
+    torch = pytest.importorskip("torch")
+    abi = pkg._abi
+    lib = abi.load()
+    prob = pkg.workloads.sinsin_square()  # 64 cells, N = 16
+    n = prob["corners"].shape[0]
+    corners_d = torch.from_numpy(prob["corners"]).cuda()
+    d = device_desc(abi, prob, corners_d, abi.PREC_FP64, 1e-10)
+    out = [torch.empty(s, dtype=t, device="cuda") for s, t in
+           (((n, 4, 4), torch.float64), ((n, 4), torch.float64), ((n,), torch.int32))]
+    args = (ctypes.byref(d), out[0].data_ptr(), out[1].data_ptr(), None, out[2].data_ptr(), None, None)
+    assert lib.msfem_run_batch_noalloc(*args) == abi.OK
+    torch.cuda.synchronize()
+    alloc0 = torch.cuda.memory_allocated()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        assert lib.msfem_run_batch_noalloc(*args) == abi.OK
+    torch.cuda.synchronize()
+    assert torch.cuda.memory_allocated() == alloc0
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 >= free0, (free0, free1)
+    assert np.all(out[2].cpu().numpy() == abi.CELL_CONVERGED)
 
 
 def test_noalloc_tabulated_coefficient(pkg, engine):
@@ -117,3 +150,8 @@ def test_noalloc_rejects_what_it_cannot_do(pkg):
     d.memory = abi.MEM_HOST
     rc = lib.msfem_run_batch_noalloc(ctypes.byref(d), 1, 1, None, 1, None, None)
     assert rc == abi.ERR_INVALID_ARG
+    d.memory = abi.MEM_DEVICE
+    d.warm_start = abi.WARM_SURROGATE  # the network lives in a handle
+    rc = lib.msfem_run_batch_noalloc(ctypes.byref(d), 1, 1, None, 1, None, None)
+    assert rc == abi.ERR_UNSUPPORTED
+    assert "MSFEM_WARM_SURROGATE" in abi.last_error(lib)
