@@ -57,7 +57,7 @@
 extern "C" {
 #endif
 
-#define MSFEM_ABI_VERSION 1
+#define MSFEM_ABI_VERSION 2
 
 /* Largest supported local refinement per coarse cell. */
 #define MSFEM_MAX_N_2D 32
@@ -149,13 +149,29 @@ typedef struct msfem_batch_desc {
   const double *corners;        /* [n_cells][2^dim][dim] */
   const int32_t *n_fine_per_cell; /* optional, [n_cells] (uneven local refinement) */
   msfem_coef_desc coef;
-  double f_value;               /* constant right-hand side f (reference: 2.0) */
-  double tol;                   /* relative l2 residual tolerance ||b-Ax||/||b|| */
+  double f_value;               /* constant right-hand side f (reference: 2.0); see f_qp_values */
+  double tol;                   /* l2 residual tolerance, relative or absolute (tol_absolute) */
   int32_t maxit;                /* CG iteration cap per solve (reference: 1000) */
   int32_t memory;               /* msfem_memory */
   int32_t warm_start;           /* msfem_warm_start */
   int32_t check_interval;       /* residual-norm check every k iterations, 0 = tuned default */
   const double *warm_basis;     /* [n_cells][2^dim][n^dim], WARM_USER only; uneven N: cell blocks of 2^d (N_c+1)^d */
+  /* Stopping rule of every solve.  0: relative, ||b - A x|| <= tol ||b||.
+   * 1: absolute, ||b - A x|| <= tol, the reference's SolverControl(1000, 1e-12)
+   * (diffusion_problem_basis.tpp:297, deal.II SolverCG checks the l2 norm of
+   * the unpreconditioned residual, from step 0).  The residual is that of the
+   * interior rows of the unscaled fine Q1 system with the Dirichlet lifting. */
+  int32_t tol_absolute;
+  int32_t reserved0;            /* must be 0 */
+  /* Optional right-hand side f at the Gauss points, replacing f_value:
+   * RightHandSide<dim>::value_list at the QGauss(2) points of every fine cell
+   * (diffusion_problem_basis.tpp:204-205, :219-220; right_hand_side.tpp:27-40).
+   * Per cell a block of 2^d N^d doubles ordered [q][fine cell] (the scalar
+   * TABULATED layout); f_qp_offset[cell] = start of the cell's block in
+   * doubles, NULL = packed blocks in cell order.  f only enters the coarse
+   * load F (the local problems have a zero right-hand side, :455). */
+  const double *f_qp_values;
+  const int64_t *f_qp_offset;
 } msfem_batch_desc;
 
 typedef struct msfem_stats {

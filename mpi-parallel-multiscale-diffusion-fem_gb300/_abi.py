@@ -85,6 +85,10 @@ class BatchDesc(ctypes.Structure):
         ("warm_start", ctypes.c_int32),
         ("check_interval", ctypes.c_int32),
         ("warm_basis", ctypes.c_void_p),
+        ("tol_absolute", ctypes.c_int32),
+        ("reserved0", ctypes.c_int32),
+        ("f_qp_values", ctypes.c_void_p),
+        ("f_qp_offset", ctypes.c_void_p),
     ]
 
 

@@ -26,7 +26,10 @@ struct KernelParams {
   const double *qp_values;
   const int64_t *qp_offset;    // nullptr = uniform cell blocks
   double f_value;
-  double tol;                  // relative residual tolerance
+  const double *f_qp;          // f at the Gauss points [q][fine cell] per cell, nullptr = f_value
+  const int64_t *f_qp_offset;  // nullptr = uniform cell blocks of 2^d N^d
+  double tol;                  // residual tolerance (relative, or absolute with tol_abs)
+  int tol_abs;                 // 1: stop at ||r|| <= tol, 0: at ||r|| <= tol ||b||
   int maxit;
   int check_interval;          // 0 = adaptive
   const double *warm_basis;    // nullptr = cold start

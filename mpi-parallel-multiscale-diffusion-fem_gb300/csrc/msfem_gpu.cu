@@ -78,6 +78,7 @@ struct msfem_handle {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   // inputs staged from the host / internal scratch
   DevBuf corners, nfine, order, queue, qp, qpoff, warm, boff, modes, spheres, sgrid_start, sgrid_ids;
+  DevBuf fqp, fqpoff;  // right-hand side tabulated at the Gauss points
   // outputs staged to the host / internal
   DevBuf M, F, basis, status, iters, relres, refine;
   DevBuf work;  // per-CTA workspace slots of the 3D kernels
@@ -378,6 +379,10 @@ int validate(const msfem_batch_desc *d) {
     return fail(MSFEM_ERR_INVALID_ARG, "unknown warm_start");
   if (d->warm_start == MSFEM_WARM_USER && d->n_cells > 0 && !d->warm_basis)
     return fail(MSFEM_ERR_INVALID_ARG, "warm_basis is NULL");
+  if (d->tol_absolute != 0 && d->tol_absolute != 1) return fail(MSFEM_ERR_INVALID_ARG, "tol_absolute must be 0 or 1");
+  if (d->reserved0 != 0) return fail(MSFEM_ERR_INVALID_ARG, "reserved0 must be 0");
+  if (d->f_qp_offset && !d->f_qp_values)
+    return fail(MSFEM_ERR_INVALID_ARG, "f_qp_offset given without f_qp_values");
   const msfem_coef_desc &c = d->coef;
   switch (c.kind) {
   case MSFEM_COEF_CONSTANT:
@@ -569,7 +574,10 @@ int msfem_run_batch_noalloc(const msfem_batch_desc *d, double *M, double *F, dou
   p.qp_values = d->coef.qp_values;
   p.qp_offset = d->coef.qp_offset;
   p.f_value = d->f_value;
+  p.f_qp = d->f_qp_values;
+  p.f_qp_offset = d->f_qp_offset;
   p.tol = d->tol;
+  p.tol_abs = d->tol_absolute;
   p.maxit = d->maxit;
   p.check_interval = d->check_interval;
   p.inner_tol = Tune().inner_tol;
@@ -637,7 +645,7 @@ int msfem_destroy(msfem_handle *h) {
   if (!h) return MSFEM_OK;
   cudaSetDevice(h->device);
   cudaStreamSynchronize(h->stream);
-  DevBuf *bufs[] = {&h->corners, &h->nfine, &h->order, &h->queue, &h->qp, &h->qpoff, &h->warm,
+  DevBuf *bufs[] = {&h->corners, &h->nfine, &h->order, &h->queue, &h->qp, &h->qpoff, &h->fqp, &h->fqpoff, &h->warm,
                     &h->boff, &h->modes, &h->spheres, &h->sgrid_start, &h->sgrid_ids,
                     &h->M, &h->F, &h->basis, &h->status, &h->iters, &h->relres, &h->refine,
                     &h->work};
@@ -1253,6 +1261,47 @@ int prepare_inputs(msfem_handle *h, const msfem_batch_desc *d, const std::vector
     p.qp_values = h->qp.as<double>();
     p.qp_offset = od;
   }
+  // right-hand side at the Gauss points: blocks of 2^d N_c^d per cell
+  p.f_qp = nullptr;
+  p.f_qp_offset = nullptr;
+  if (d->f_qp_values && nc > 0) {
+    std::vector<int64_t> off;
+    int64_t total = 0;
+    if (d->f_qp_offset) {
+      off.resize(nc);
+      if (dev) {
+        MSFEM_CUDA(cudaMemcpyAsync(off.data(), d->f_qp_offset, sizeof(int64_t) * nc, cudaMemcpyDeviceToHost,
+                                   h->stream));
+        MSFEM_CUDA(cudaStreamSynchronize(h->stream));
+      } else {
+        std::memcpy(off.data(), d->f_qp_offset, sizeof(int64_t) * nc);
+      }
+      for (int c = 0; c < nc; ++c) {
+        if (off[c] < 0) return fail(MSFEM_ERR_INVALID_ARG, "f_qp_offset[" + std::to_string(c) + "] < 0");
+        total = std::max(total, off[c] + (int64_t)nv * ipow(cell_N(d, nf, c), dim));
+      }
+    } else if (d->n_fine_per_cell) {
+      off.resize(nc);
+      for (int c = 0; c < nc; ++c) {
+        off[c] = total;
+        total += (int64_t)nv * ipow(nf[c], dim);
+      }
+    } else {
+      total = (int64_t)nc * nv * ipow(d->n_fine, dim);
+    }
+    const double *fq = nullptr;
+    if ((rc = upload<double>(h, h->fqp, d->f_qp_values, (size_t)total, dev, &fq, &h2d))) return rc;
+    p.f_qp = fq;
+    if (!off.empty()) {
+      const int64_t *od = nullptr;
+      if (d->f_qp_offset && dev) {
+        od = d->f_qp_offset;
+      } else if ((rc = upload<int64_t>(h, h->fqpoff, off.data(), off.size(), false, &od, &h2d))) {
+        return rc;
+      }
+      p.f_qp_offset = od;
+    }
+  }
   p.basis_offset = boffd;
   return MSFEM_OK;
 }
@@ -1297,6 +1346,7 @@ int run_batch_impl(msfem_handle *h, const msfem_batch_desc *d, double *M, double
   int64_t basis_total = 0;
   if ((rc = prepare_inputs(h, d, nf, p, basis_total, h2d, launches))) return rc;
   p.tol = d->tol;
+  p.tol_abs = d->tol_absolute;
   p.maxit = d->maxit;
   p.check_interval = d->check_interval > 0 ? d->check_interval : tn.check_interval;
   p.inner_tol = tn.inner_tol;

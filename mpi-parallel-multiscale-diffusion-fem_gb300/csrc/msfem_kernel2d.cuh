@@ -102,6 +102,7 @@ struct CellShared2D {
   double jfine[4];    // affine cells: fine-cell Jacobian, columns dx/dxi, dx/deta
   double absdet;      // affine cells: |det J_fine|
   double bb[4];       // ||b_i||^2 (unscaled)
+  double bthr[4];     // stopping scale: ||b_i||^2 (relative tolerance) or 1 (absolute)
   double nu[4];       // last ||r_i||^2 (unscaled)
   double rho[4];
   double alpha[4];
@@ -431,14 +432,19 @@ __device__ __forceinline__ void boundary_value(const CellShared2D &cs, const dou
   for (int r = 0; r < 4; ++r) t[r] = gv[r] * sq;
 }
 
-// Load vector b_k = f int psi_k at node (ix, iy).  Affine cells: every fine
-// cell carries f |det| / 4 to each of its vertices; general cells: QGauss(2)
-// over the adjacent fine cells.
+// Load vector b_k = int f psi_k at node (ix, iy) (diffusion_problem_basis.tpp:
+// 219-220): QGauss(2) over the adjacent fine cells.  Constant f on affine
+// cells: every fine cell carries f |det| / 4 to each of its vertices.  With f
+// tabulated at the Gauss points (p.f_qp), or on general cells, the quadrature
+// sum itself, with the per-point |det J| on general cells.
 __device__ inline double node_load(const KernelParams &p, const CellShared2D &cs, int N, int ix, int iy) {
-  if (cs.affine) {
+  if (cs.affine && !p.f_qp) {
     const double m = (ix == 0 || ix == N ? 1.0 : 2.0) * (iy == 0 || iy == N ? 1.0 : 2.0);
     return p.f_value * 0.25 * cs.absdet * m;
   }
+  const double *fq = nullptr;
+  const int nfc = N * N;
+  if (p.f_qp) fq = p.f_qp + (p.f_qp_offset ? p.f_qp_offset[cs.cell] : (int64_t)cs.cell * 4 * nfc);
   const double invN = 1.0 / (double)N;
   double b = 0.0;
   for (int dy = -1; dy <= 0; ++dy)
@@ -446,25 +452,33 @@ __device__ inline double node_load(const KernelParams &p, const CellShared2D &cs
       const int cx = ix + dx, cy = iy + dy;
       if (cx < 0 || cy < 0 || cx >= N || cy >= N) continue;
       const int kx = ix - cx, ky = iy - cy;  // local vertex of the node
+      const int fc = cy * N + cx;
       double V[8];
-      bilinear_map(cs.corners, cx * invN, cy * invN, V + 0);
-      bilinear_map(cs.corners, (cx + 1) * invN, cy * invN, V + 2);
-      bilinear_map(cs.corners, cx * invN, (cy + 1) * invN, V + 4);
-      bilinear_map(cs.corners, (cx + 1) * invN, (cy + 1) * invN, V + 6);
+      if (!cs.affine) {
+        bilinear_map(cs.corners, cx * invN, cy * invN, V + 0);
+        bilinear_map(cs.corners, (cx + 1) * invN, cy * invN, V + 2);
+        bilinear_map(cs.corners, cx * invN, (cy + 1) * invN, V + 4);
+        bilinear_map(cs.corners, (cx + 1) * invN, (cy + 1) * invN, V + 6);
+      }
       for (int q = 0; q < 4; ++q) {
         const int qx = q & 1, qy = q >> 1;
-        double J00 = 0, J01 = 0, J10 = 0, J11 = 0;
-        for (int k = 0; k < 4; ++k) {
-          const int vx = k & 1, vy = k >> 1;
-          const double gx = (vx ? 1.0 : -1.0) * lval(vy, qy);
-          const double gy = (vy ? 1.0 : -1.0) * lval(vx, qx);
-          J00 += V[2 * k] * gx; J01 += V[2 * k] * gy;
-          J10 += V[2 * k + 1] * gx; J11 += V[2 * k + 1] * gy;
+        double det = cs.absdet;
+        if (!cs.affine) {
+          double J00 = 0, J01 = 0, J10 = 0, J11 = 0;
+          for (int k = 0; k < 4; ++k) {
+            const int vx = k & 1, vy = k >> 1;
+            const double gx = (vx ? 1.0 : -1.0) * lval(vy, qy);
+            const double gy = (vy ? 1.0 : -1.0) * lval(vx, qx);
+            J00 += V[2 * k] * gx; J01 += V[2 * k] * gy;
+            J10 += V[2 * k + 1] * gx; J11 += V[2 * k + 1] * gy;
+          }
+          det = fabs(J00 * J11 - J01 * J10);
         }
-        b += lval(kx, qx) * lval(ky, qy) * 0.25 * fabs(J00 * J11 - J01 * J10);
+        const double f = fq ? fq[q * nfc + fc] : p.f_value;
+        b += f * lval(kx, qx) * lval(ky, qy) * 0.25 * det;
       }
     }
-  return p.f_value * b;
+  return b;
 }
 
 // Epilogue contribution of node (ix, iy) with y = A~ phi~ known there.
@@ -618,7 +632,10 @@ msfem2d_kernel(const KernelParams p) {
     __syncthreads();
     if (warp == 0) {
       const double t = warp_finish<4>(red[1], NW, lane);
-      if (lane < 4) cs.bb[lane] = t;
+      if (lane < 4) {
+        cs.bb[lane] = t;
+        cs.bthr[lane] = p.tol_abs ? 1.0 : t;
+      }
     }
     // warm start: x~0 = D^1/2 phi_warm on the interior, r0 = -(A~ phi~0)_I
     const bool warm = p.warm_basis != nullptr;
@@ -680,7 +697,7 @@ msfem2d_kernel(const KernelParams p) {
       const double nu = shfl_xor_d(t, 4);  // lane r (<4) gets value 4+r
       if (lane < 4) {
         cs.rho[lane] = t;
-        const bool conv = nu <= tol2 * cs.bb[lane];
+        const bool conv = nu <= tol2 * cs.bthr[lane];
         cs.active[lane] = !conv;
         cs.iters[lane] = 0;
         cs.beta[lane] = 0.0;
@@ -690,7 +707,7 @@ msfem2d_kernel(const KernelParams p) {
         int any = 0, nn2 = 0;
         for (int r = 0; r < 4; ++r) {
           any |= cs.active[r];
-          if (cs.active[r] && cs.dmin * cs.rho[r] <= 100.0 * tol2 * cs.bb[r]) nn2 = 1;
+          if (cs.active[r] && cs.dmin * cs.rho[r] <= 100.0 * tol2 * cs.bthr[r]) nn2 = 1;
         }
         cs.done = !any;
         cs.need_nu = nn2 || p.check_interval == 1;
@@ -777,7 +794,7 @@ msfem2d_kernel(const KernelParams p) {
             if (!isfinite(t)) {
               cs.active[lane] = 0;
               cs.iters[lane] = -it;
-            } else if (t == 0.0 || (need_nu && nu <= tol2 * cs.bb[lane])) {
+            } else if (t == 0.0 || (need_nu && nu <= tol2 * cs.bthr[lane])) {
               cs.active[lane] = 0;
               cs.iters[lane] = it;
             } else if (it >= p.maxit) {
@@ -795,7 +812,7 @@ msfem2d_kernel(const KernelParams p) {
           int any = 0, nn2 = 0;
           for (int r = 0; r < 4; ++r) {
             any |= cs.active[r];
-            if (cs.active[r] && cs.dmin * cs.rho[r] <= 100.0 * tol2 * cs.bb[r]) nn2 = 1;
+            if (cs.active[r] && cs.dmin * cs.rho[r] <= 100.0 * tol2 * cs.bthr[r]) nn2 = 1;
           }
           cs.done = !any;
           cs.need_nu = nn2 || (p.check_interval > 0 && ((it + 1) % p.check_interval) == 0);
@@ -1038,7 +1055,10 @@ msfem2d_mixed_kernel(const KernelParams p) {
     __syncthreads();
     if (warp == 0) {
       const double t = warp_finish<4>(red[1], NW, lane);
-      if (lane < 4) cs.bb[lane] = t;
+      if (lane < 4) {
+        cs.bb[lane] = t;
+        cs.bthr[lane] = p.tol_abs ? 1.0 : t;
+      }
     }
     if (p.warm_basis != nullptr) {
       const double *wb = p.warm_basis + (p.basis_offset ? p.basis_offset[cell] : (int64_t)cell * 4 * n * n);
@@ -1145,7 +1165,7 @@ msfem2d_mixed_kernel(const KernelParams p) {
             cs.active[lane] = 0;
             cs.iters[lane] = -1;
           } else {
-            cs.active[lane] = !(t <= tol2 * cs.bb[lane]);
+            cs.active[lane] = !(t <= tol2 * cs.bthr[lane]);
           }
         }
         __syncwarp();
@@ -1192,7 +1212,7 @@ msfem2d_mixed_kernel(const KernelParams p) {
   #pragma unroll
         for (int r = 0; r < 4; ++r) {
           iact[r] = act[r] > 0.0f && rho[r] > 0.0f;
-          const double goal = cs.nu[r] > 0.0 ? 0.01 * tol2 * cs.bb[r] / cs.nu[r] : 0.0;
+          const double goal = cs.nu[r] > 0.0 ? 0.01 * tol2 * cs.bthr[r] / cs.nu[r] : 0.0;
           itol2r[r] = fmaxf(itol2, (float)fmin(goal, 0.25));
         }
         int iit = 0;
@@ -1369,7 +1389,7 @@ msfem2d_mixed_kernel(const KernelParams p) {
           rho[r] = rzrr[r];
           rho0[r] = rzrr[4 + r];
           iact[r] = act[r] > 0.0f && rho0[r] > 0.0f && rho[r] > 0.0f;
-          const double goal = cs.nu[r] > 0.0 ? 0.01 * tol2 * cs.bb[r] / cs.nu[r] : 0.0;
+          const double goal = cs.nu[r] > 0.0 ? 0.01 * tol2 * cs.bthr[r] / cs.nu[r] : 0.0;
           itol2r[r] = fmaxf(itol2, (float)fmin(goal, 0.25));
         }
 #pragma unroll

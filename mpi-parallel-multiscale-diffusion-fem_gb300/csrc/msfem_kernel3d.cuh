@@ -84,6 +84,7 @@ struct CellShared3D {
   double absdet;
   double tmpl[8][36];  // affine scalar coefficient: K = sum_q a_q tmpl[q] (upper triangle)
   double bb[8];
+  double bthr[8];      // stopping scale: ||b_i||^2 (relative tolerance) or 1 (absolute)
   double nu[8];
   double rho[8];
   double alpha[8];
@@ -822,7 +823,10 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
           }
 #pragma unroll
         for (int mm = 8; mm < 32; mm <<= 1) s += shfl_xor_d(s, mm);
-        if (lane < 8) cs.bb[lane] = s;
+        if (lane < 8) {
+          cs.bb[lane] = s;
+          cs.bthr[lane] = p.tol_abs ? 1.0 : s;
+        }
       }
     }
     // warm start: x~0 = D^1/2 phi_warm, r = -(A~ phi~0)_I
@@ -886,7 +890,7 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
         const double nu = shfl_xor_d(s, 8);
         if (lane < 8) {
           cs.rho[lane] = s;
-          cs.active[lane] = !(nu <= tol2 * cs.bb[lane]);
+          cs.active[lane] = !(nu <= tol2 * cs.bthr[lane]);
           cs.iters[lane] = 0;
         }
         __syncwarp();
@@ -894,7 +898,7 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
           int any = 0, nn2 = 0;
           for (int r = 0; r < 8; ++r) {
             any |= cs.active[r];
-            if (cs.active[r] && cs.dmin * cs.rho[r] <= 100.0 * tol2 * cs.bb[r]) nn2 = 1;
+            if (cs.active[r] && cs.dmin * cs.rho[r] <= 100.0 * tol2 * cs.bthr[r]) nn2 = 1;
           }
           cs.done = !any;
           cs.need_nu = nn2 || p.check_interval == 1;
@@ -987,7 +991,7 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
               if (!isfinite(s)) {
                 cs.active[lane] = 0;
                 cs.iters[lane] = -it;
-              } else if (s == 0.0 || (need_nu && nu <= tol2 * cs.bb[lane])) {
+              } else if (s == 0.0 || (need_nu && nu <= tol2 * cs.bthr[lane])) {
                 cs.active[lane] = 0;
                 cs.iters[lane] = it;
               } else if (it >= p.maxit) {
@@ -1005,7 +1009,7 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
             int any = 0, nn2 = 0;
             for (int r = 0; r < 8; ++r) {
               any |= cs.active[r];
-              if (cs.active[r] && cs.dmin * cs.rho[r] <= 100.0 * tol2 * cs.bb[r]) nn2 = 1;
+              if (cs.active[r] && cs.dmin * cs.rho[r] <= 100.0 * tol2 * cs.bthr[r]) nn2 = 1;
             }
             cs.done = !any;
             cs.need_nu = nn2 || (p.check_interval > 0 && ((it + 1) % p.check_interval) == 0);
@@ -1062,7 +1066,7 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
               cs.active[lane] = 0;
               cs.iters[lane] = -1;
             } else {
-              cs.active[lane] = !(s <= tol2 * cs.bb[lane]);
+              cs.active[lane] = !(s <= tol2 * cs.bthr[lane]);
             }
           }
           __syncwarp();
@@ -1133,7 +1137,7 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
         for (int r = 0; r < 8; ++r) {
           if (act[r] > 0.0f && rho[r] > 0.0f) iact |= 1u << r;
           // never deeper than the outer goal needs (factor 10 margin)
-          const double goal = cs.nu[r] > 0.0 ? 0.01 * tol2 * cs.bb[r] / cs.nu[r] : 0.0;
+          const double goal = cs.nu[r] > 0.0 ? 0.01 * tol2 * cs.bthr[r] / cs.nu[r] : 0.0;
           thr[r] = fmaxf(itol2, (float)fmin(goal, 0.25)) * rho[r];
         }
         if (tid < 8) {
@@ -1209,35 +1213,46 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
           }
         } else {
           // load vector b_k (affine: f |det| / 8 per adjacent fine cell)
+          // b_k = int f psi_k (diffusion_problem_basis.tpp:219-220)
           double bl;
-          if (cs.affine) {
+          if (cs.affine && !p.f_qp) {
             const double mult = (ix == 0 || ix == N ? 1.0 : 2.0) * (iy == 0 || iy == N ? 1.0 : 2.0) *
                                 (iz == 0 || iz == N ? 1.0 : 2.0);
             bl = fj * 0.125 * cs.absdet * mult;
           } else {
+            // QGauss(2) over the adjacent fine cells: f tabulated at the Gauss
+            // points (p.f_qp) or constant; per-point |det J| on general cells
             const double invN = 1.0 / (double)N;
+            const int nfc = N * N * N;
+            const double *fq =
+                p.f_qp ? p.f_qp + (p.f_qp_offset ? p.f_qp_offset[cell] : (int64_t)cell * 8 * nfc) : nullptr;
             bl = 0.0;
             for (int c8 = 0; c8 < 8; ++c8) {
               const int cx = ix - (c8 & 1), cy = iy - ((c8 >> 1) & 1), cz = iz - (c8 >> 2);
               if (cx < 0 || cy < 0 || cz < 0 || cx >= N || cy >= N || cz >= N) continue;
               const int kv = (c8 & 1) + 2 * ((c8 >> 1) & 1) + 4 * (c8 >> 2);  // local vertex
+              const int fc = (cz * N + cy) * N + cx;
               double V[24];
-              for (int k8 = 0; k8 < 8; ++k8) {
-                const double t[3] = {(cx + (k8 & 1)) * invN, (cy + ((k8 >> 1) & 1)) * invN, (cz + (k8 >> 2)) * invN};
-                trilinear_map(cs.corners, t, V + 3 * k8);
-              }
+              if (!cs.affine)
+                for (int k8 = 0; k8 < 8; ++k8) {
+                  const double t[3] = {(cx + (k8 & 1)) * invN, (cy + ((k8 >> 1) & 1)) * invN, (cz + (k8 >> 2)) * invN};
+                  trilinear_map(cs.corners, t, V + 3 * k8);
+                }
               for (int q = 0; q < 8; ++q) {
-                double J[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-                for (int k8 = 0; k8 < 8; ++k8)
-                  for (int a = 0; a < 3; ++a)
-                    for (int c = 0; c < 3; ++c) J[3 * a + c] += V[3 * k8 + a] * rgrad(k8, q, c);
-                const double det = J[0] * (J[4] * J[8] - J[5] * J[7]) + J[1] * (J[5] * J[6] - J[3] * J[8]) +
-                                   J[2] * (J[3] * J[7] - J[4] * J[6]);
+                double det = cs.absdet;
+                if (!cs.affine) {
+                  double J[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+                  for (int k8 = 0; k8 < 8; ++k8)
+                    for (int a = 0; a < 3; ++a)
+                      for (int c = 0; c < 3; ++c) J[3 * a + c] += V[3 * k8 + a] * rgrad(k8, q, c);
+                  det = fabs(J[0] * (J[4] * J[8] - J[5] * J[7]) + J[1] * (J[5] * J[6] - J[3] * J[8]) +
+                             J[2] * (J[3] * J[7] - J[4] * J[6]));
+                }
                 const double psi = lv3(kv & 1, q & 1) * lv3((kv >> 1) & 1, (q >> 1) & 1) * lv3(kv >> 2, q >> 2);
-                bl += psi * 0.125 * fabs(det);
+                const double f = fq ? fq[q * nfc + fc] : fj;
+                bl += f * psi * 0.125 * det;
               }
             }
-            bl *= fj;
           }
           const double d = d64[g];
           const double s = rsqrt(d);

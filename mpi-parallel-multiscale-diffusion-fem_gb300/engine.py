@@ -61,9 +61,11 @@ class Engine:
     # -- descriptor -------------------------------------------------------
     @staticmethod
     def make_desc(problem, precision="fp64", tol=1e-10, maxit=1000, check_interval=0,
-                  warm_basis=None, memory=_abi.MEM_HOST, keep=None):
+                  warm_basis=None, memory=_abi.MEM_HOST, keep=None, tol_absolute=False):
         """msfem_batch_desc for host numpy data (memory=HOST).  `keep`
-        collects the arrays whose buffers the descriptor points to."""
+        collects the arrays whose buffers the descriptor points to.  The
+        problem's optional "f_qp_values" / "f_qp_offset" tabulate f at the
+        Gauss points; tol_absolute selects the reference's absolute stop."""
         keep = [] if keep is None else keep
         d = _abi.BatchDesc()
         d.dim = problem["dim"]
@@ -101,7 +103,13 @@ class Engine:
             d.coef.spheres = _ptr(sp)
             d.coef.n_spheres = sp.shape[0]
         d.f_value = float(problem.get("f_value", 1.0))
+        for key in ("f_qp_values", "f_qp_offset"):
+            if problem.get(key) is not None:
+                arr = np.ascontiguousarray(problem[key], dtype=np.int64 if key == "f_qp_offset" else np.float64)
+                keep.append(arr)
+                setattr(d, key, _ptr(arr))
         d.tol = float(tol)
+        d.tol_absolute = int(bool(tol_absolute))
         d.maxit = int(maxit)
         d.memory = memory
         d.check_interval = int(check_interval)
@@ -122,9 +130,10 @@ class Engine:
 
     # -- calls --------------------------------------------------------------
     def run(self, problem, precision="fp64", tol=1e-10, maxit=1000, want_basis=False,
-            warm_basis=None, check_interval=0, raise_on_failure=False):
+            warm_basis=None, check_interval=0, raise_on_failure=False, tol_absolute=False):
         keep = []
-        d = self.make_desc(problem, precision, tol, maxit, check_interval, warm_basis, keep=keep)
+        d = self.make_desc(problem, precision, tol, maxit, check_interval, warm_basis, keep=keep,
+                           tol_absolute=tol_absolute)
         nc, nv = d.n_cells, 1 << d.dim
         M = np.zeros((nc, nv, nv))
         F = np.zeros((nc, nv))

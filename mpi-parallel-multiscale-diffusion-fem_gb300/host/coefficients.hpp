@@ -44,6 +44,11 @@ class ScalarFunction {
     if (points.size() != values.size()) throw std::invalid_argument("value_list: size mismatch");
     for (size_t i = 0; i < points.size(); ++i) values[i] = value(points[i], component);
   }
+  // A constant function reports its value (no tabulation needed).
+  virtual bool constant_value(double &v) const {
+    (void)v;
+    return false;
+  }
 };
 
 // MatrixCoeff<dim>, include/coefficients/matrix_coeff.tpp:17-91:
@@ -131,6 +136,10 @@ class RightHandSide : public ScalarFunction<dim> {
   explicit RightHandSide(double f = 2.0) : f_(f) {}
   double value(const Point<dim> &, unsigned int = 0) const override { return f_; }
   double constant() const { return f_; }
+  bool constant_value(double &v) const override {
+    v = f_;
+    return true;
+  }
 
  private:
   double f_;

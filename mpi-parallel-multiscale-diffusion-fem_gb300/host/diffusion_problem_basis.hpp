@@ -46,9 +46,18 @@ class BasisBatch {
   // Problem data used by every flush (the reference hard-codes MatrixCoeff
   // and RightHandSide inside assemble_system, diffusion_problem_basis.tpp:182-188).
   void set_coefficient(std::shared_ptr<Coefficients::TensorFunction2<dim>> c) { coef_ = std::move(c); }
-  void set_right_hand_side(double f) { f_ = f; }
+  // Any Function<dim>: a constant one is passed as f_value, any other is
+  // tabulated at the QGauss(2) points through value_list.
+  void set_right_hand_side(std::shared_ptr<Coefficients::ScalarFunction<dim>> f) { rhs_ = std::move(f); }
+  void set_right_hand_side(double f) { rhs_ = std::make_shared<Coefficients::RightHandSide<dim>>(f); }
   void set_precision(int precision) { precision_ = precision; }
-  void set_tolerance(double tol, int maxit) { tol_ = tol; maxit_ = maxit; }
+  // absolute = true is the reference's SolverControl(maxit, tol) stop on the
+  // l2 norm of the residual; false stops at tol times ||b||.
+  void set_tolerance(double tol, int maxit, bool absolute = true) {
+    tol_ = tol;
+    maxit_ = maxit;
+    tol_absolute_ = absolute;
+  }
   void set_device(int device) { device_ = device; }
   const msfem_stats &last_stats() const { return stats_; }
 
@@ -60,13 +69,39 @@ class BasisBatch {
   void flush();
 
  private:
-  BasisBatch() : coef_(std::make_shared<Coefficients::MatrixCoeff<dim>>()) {}
+  BasisBatch()
+      : coef_(std::make_shared<Coefficients::MatrixCoeff<dim>>()),
+        rhs_(std::make_shared<Coefficients::RightHandSide<dim>>()) {}
+  // Gauss points (QGauss(2), x fastest) of every fine cell of a cell with
+  // corners cr[2^dim][dim] and N fine cells per direction, for point q.
+  static void gauss_points(const double *cr, int N, int q, std::vector<Point<dim>> &pts) {
+    constexpr int nv = GeometryInfo<dim>::vertices_per_cell;
+    const double g[2] = {0.5 - 0.5 / std::sqrt(3.0), 0.5 + 0.5 / std::sqrt(3.0)};
+    const int nfc = dim == 2 ? N * N : N * N * N;
+    pts.resize((size_t)nfc);
+    for (int fc = 0; fc < nfc; ++fc) {
+      const int ci[3] = {fc % N, (fc / N) % N, dim == 3 ? fc / (N * N) : 0};
+      double t[3], x[3] = {0, 0, 0};
+      for (int a = 0; a < dim; ++a) t[a] = (ci[a] + g[(q >> a) & 1]) / N;
+      for (int v = 0; v < nv; ++v) {
+        double w = 1.0;
+        for (int a = 0; a < dim; ++a) w *= ((v >> a) & 1) ? t[a] : 1.0 - t[a];
+        for (int a = 0; a < dim; ++a) x[a] += w * cr[v * dim + a];
+      }
+      Point<dim> p;
+      for (int a = 0; a < dim; ++a) p(a) = x[a];
+      pts[fc] = p;
+    }
+  }
   msfem_handle *handle_ = nullptr;
   std::vector<DiffusionProblemBasis<dim> *> pending_;
   std::shared_ptr<Coefficients::TensorFunction2<dim>> coef_;
-  double f_ = 2.0;  // Coefficients::RightHandSide, right_hand_side.tpp:22
+  // Coefficients::RightHandSide, f = 2 (right_hand_side.tpp:22)
+  std::shared_ptr<Coefficients::ScalarFunction<dim>> rhs_;
   int precision_ = MSFEM_PREC_FP64;
-  double tol_ = 1e-12;  // SolverControl(1000, 1e-12), diffusion_problem_basis.tpp:297
+  // SolverControl(1000, 1e-12), diffusion_problem_basis.tpp:297: absolute l2 residual
+  double tol_ = 1e-12;
+  bool tol_absolute_ = true;
   int maxit_ = 1000;
   int device_ = 0;
   msfem_stats stats_{};
@@ -159,8 +194,24 @@ class DiffusionProblemBasis {
                       sub + ".cell-" + global_cell_id.to_string() + ".vtu";
   }
 
-  // Plain VTU of the local fine grid with one point field (replaces DataOut).
-  void write_vtu(const std::string &name, const Vector &field) const {
+  // diffusion_problem_basis.tpp:392-418: every basis function of the cell
+  // as point data basis_0 .. basis_{2^dim-1} in "2d-basis.<subdomain>.cell-<id>.vtu"
+  // ("3d-..." in 3D).  The subdomain field is that of the local serial
+  // Triangulation, whose locally_owned_subdomain() is
+  // numbers::invalid_subdomain_id (4294967295), as in the reference.
+  void output_basis() const {
+    std::string name = std::string(dim == 2 ? "2d-" : "3d-") + "basis." + std::to_string(4294967295u) +
+                       ".cell-" + global_cell_id.to_string() + ".vtu";
+    std::vector<std::pair<std::string, const Vector *>> fields;
+    for (unsigned int i = 0; i < GeometryInfo<dim>::vertices_per_cell; ++i)
+      fields.emplace_back("basis_" + std::to_string(i), &solution_vector[i]);
+    write_vtu(name, fields);
+  }
+
+  void write_vtu(const std::string &name, const Vector &field) const { write_vtu(name, {{"solution", &field}}); }
+
+  // Plain VTU of the local fine grid with point fields (replaces DataOut).
+  void write_vtu(const std::string &name, const std::vector<std::pair<std::string, const Vector *>> &fields) const {
     const unsigned int N = n_fine(), n = N + 1;
     const size_t nn = n_nodes(), nc = dim == 2 ? size_t(N) * N : size_t(N) * N * N;
     std::ofstream out(name);
@@ -194,10 +245,14 @@ class DiffusionProblemBasis {
     for (size_t c = 0; c < nc; ++c) out << (c + 1) * npc << '\n';
     out << "</DataArray>\n<DataArray type=\"UInt8\" Name=\"types\" format=\"ascii\">\n";
     for (size_t c = 0; c < nc; ++c) out << (dim == 2 ? 9 : 12) << '\n';
-    out << "</DataArray>\n</Cells>\n<PointData Scalars=\"solution\">\n";
-    out << "<DataArray type=\"Float64\" Name=\"solution\" format=\"ascii\">\n";
-    for (size_t k = 0; k < nn; ++k) out << field(k) << '\n';
-    out << "</DataArray>\n</PointData>\n</Piece>\n</UnstructuredGrid>\n</VTKFile>\n";
+    out << "</DataArray>\n</Cells>\n<PointData Scalars=\"" << fields[0].first << "\">\n";
+    out.precision(17);
+    for (const auto &f : fields) {
+      out << "<DataArray type=\"Float64\" Name=\"" << f.first << "\" format=\"ascii\">\n";
+      for (size_t k = 0; k < nn; ++k) out << (*f.second)(k) << '\n';
+      out << "</DataArray>\n";
+    }
+    out << "</PointData>\n</Piece>\n</UnstructuredGrid>\n</VTKFile>\n";
   }
 
   MPI_Comm mpi_communicator;
@@ -250,15 +305,40 @@ void BasisBatch<dim>::flush() {
   d.n_fine_per_cell = uniform ? nullptr : nf.data();
   d.precision = precision_;
   d.corners = corners.data();
-  d.f_value = f_;
   d.tol = tol_;
+  d.tol_absolute = tol_absolute_ ? 1 : 0;
   d.maxit = maxit_;
   d.memory = MSFEM_MEM_HOST;
+  // right-hand side: RightHandSide::value_list at the QGauss(2) points
+  // (diffusion_problem_basis.tpp:204-205) unless it is a constant
+  std::vector<double> ftab;
+  std::vector<int64_t> foff;
+  double fconst = 0.0;
+  if (rhs_->constant_value(fconst)) {
+    d.f_value = fconst;
+  } else {
+    foff.resize(n);
+    std::vector<Point<dim>> pts;
+    std::vector<double> vals;
+    for (int c = 0; c < n; ++c) {
+      const int N = nf[c];
+      const int nfc = dim == 2 ? N * N : N * N * N;
+      foff[c] = (int64_t)ftab.size();
+      ftab.resize(ftab.size() + (size_t)nv * nfc);
+      for (int q = 0; q < nv; ++q) {
+        gauss_points(corners.data() + (size_t)c * nv * dim, N, q, pts);
+        vals.resize(pts.size());
+        rhs_->value_list(pts, vals);
+        std::copy(vals.begin(), vals.end(), ftab.begin() + foff[c] + (size_t)q * nfc);
+      }
+    }
+    d.f_qp_values = ftab.data();
+    d.f_qp_offset = foff.data();
+  }
   std::vector<double> tab;
   std::vector<int64_t> qoff;
   if (!coef_->describe(d.coef)) {
     // generic TensorFunction: tabulate at the QGauss(2) points via value_list
-    const double g[2] = {0.5 - 0.5 / std::sqrt(3.0), 0.5 + 0.5 / std::sqrt(3.0)};
     const int ncomp = dim == 2 ? 3 : 6;
     qoff.resize(n);
     for (int c = 0; c < n; ++c) {
@@ -266,22 +346,10 @@ void BasisBatch<dim>::flush() {
       const int nfc = dim == 2 ? N * N : N * N * N;
       qoff[c] = (int64_t)tab.size();
       tab.resize(tab.size() + (size_t)ncomp * nv * nfc);
-      std::vector<Point<dim>> pts((size_t)nfc);
+      std::vector<Point<dim>> pts;
       std::vector<Tensor<2, dim>> vals((size_t)nfc);
       for (int q = 0; q < nv; ++q) {
-        for (int fc = 0; fc < nfc; ++fc) {
-          const int ci[3] = {fc % N, (fc / N) % N, dim == 3 ? fc / (N * N) : 0};
-          double t[3], x[3] = {0, 0, 0};
-          for (int a = 0; a < dim; ++a) t[a] = (ci[a] + g[(q >> a) & 1]) / N;
-          for (int v = 0; v < nv; ++v) {
-            double w = 1.0;
-            for (int a = 0; a < dim; ++a) w *= ((v >> a) & 1) ? t[a] : 1.0 - t[a];
-            for (int a = 0; a < dim; ++a) x[a] += w * corners[((size_t)c * nv + v) * dim + a];
-          }
-          Point<dim> p;
-          for (int a = 0; a < dim; ++a) p(a) = x[a];
-          pts[fc] = p;
-        }
+        gauss_points(corners.data() + (size_t)c * nv * dim, N, q, pts);
         coef_->value_list(pts, vals);
         for (int fc = 0; fc < nfc; ++fc) {
           const auto &A = vals[fc];
@@ -322,6 +390,9 @@ void BasisBatch<dim>::flush() {
       for (size_t k = 0; k < b->n_nodes(); ++k) b->solution_vector[i](k) = basis[off + i * b->n_nodes() + k];
     off += nv * b->n_nodes();
     b->is_built_global_element_matrix = true;
+    // run() writes the basis functions when output_flag is set
+    // (diffusion_problem_basis.tpp:468-471)
+    if (b->output_flag) b->output_basis();
   }
 }
 

@@ -38,6 +38,10 @@ class DiffusionProblemMultiscale {
     send_global_weights_to_cell();
   }
 
+  // The reference has no such switch (its driver never calls
+  // set_output_flag); the mock driver uses it to exercise output_basis.
+  void set_output_flag_first_cell(bool flag) { output_first_ = flag; }
+
   unsigned int n_cells_per_dir() const { return 1u << n_refine; }
   const std::vector<double> &coarse_solution() const { return u; }
   const std::map<CellId, DiffusionProblemBasis<dim>> &basis_map() const { return cell_basis_map; }
@@ -62,6 +66,7 @@ class DiffusionProblemMultiscale {
     cell_basis_map.clear();
     for (const auto &cell : cells_) {
       DiffusionProblemBasis<dim> current_cell_problem(n_refine_local, cell, 0, 0);
+      if (output_first_ && cell.id() == cells_.front().id()) current_cell_problem.set_output_flag(true);
       auto result = cell_basis_map.insert(std::make_pair(cell.id(), current_cell_problem));
       if (!result.second) throw std::logic_error("Insertion of local basis problem into std::map failed.");
     }
@@ -204,6 +209,7 @@ class DiffusionProblemMultiscale {
   int bc;
   std::vector<CoarseCell<dim>> cells_;
   std::map<CellId, DiffusionProblemBasis<dim>> cell_basis_map;
+  bool output_first_ = false;
   std::vector<double> A, rhs, u;
 };
 

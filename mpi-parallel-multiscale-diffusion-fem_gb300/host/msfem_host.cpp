@@ -13,15 +13,33 @@
 
 namespace {
 
+// A right-hand side without a constant value, f(x) = f0 + x: the batch
+// tabulates it at the Gauss points through value_list.
+template <int dim>
+class LinearRhs : public Coefficients::ScalarFunction<dim> {
+ public:
+  explicit LinearRhs(double f0) : f0_(f0) {}
+  double value(const dealii::Point<dim> &p, unsigned int = 0) const override { return f0_ + p(0); }
+
+ private:
+  double f0_;
+};
+
+enum { kOptRelativeTol = 1, kOptLinearRhs = 2, kOptOutputBasis = 4 };
+
 template <int dim>
 int run_ms(int n_refine, int n_refine_local, int coef, const double *params, double f_value, int bc,
            int precision, int device, double *u_out, double *M_out, double *F_out, double *fine_out,
-           int write_vtu) {
+           int write_vtu, int options) {
   using namespace DiffusionProblem;
   auto &batch = BasisBatch<dim>::get();
   batch.set_device(device);
   batch.set_precision(precision);
-  batch.set_right_hand_side(f_value);
+  if (options & kOptLinearRhs)
+    batch.set_right_hand_side(std::make_shared<LinearRhs<dim>>(f_value));
+  else
+    batch.set_right_hand_side(f_value);
+  batch.set_tolerance(1e-12, 1000, !(options & kOptRelativeTol));
   if (coef == 0) {
     batch.set_coefficient(std::make_shared<Coefficients::MatrixCoeff<dim>>());
   } else if (coef == 1) {
@@ -35,6 +53,7 @@ int run_ms(int n_refine, int n_refine_local, int coef, const double *params, dou
     batch.set_coefficient(std::make_shared<Coefficients::ConstantCoeff<dim>>(A));
   }
   DiffusionProblemMultiscale<dim> ms(n_refine, n_refine_local, bc);
+  ms.set_output_flag_first_cell(options & kOptOutputBasis);
   ms.run();
   const auto &u = ms.coarse_solution();
   if (u_out) std::memcpy(u_out, u.data(), sizeof(double) * u.size());
@@ -73,16 +92,20 @@ extern "C" {
 // Outputs (nullable): u [(K+1)^d] coarse solution, M [cells][2^d][2^d],
 // F [cells][2^d], fine [cells][(N+1)^d] reconstructed fine solution;
 // write_vtu: the first cell's fine solution as VTU in the working directory.
+// options: bit 0 = stop at 1e-12 relative instead of the reference's absolute
+// 1e-12; bit 1 = f(x) = f_value + x, a right-hand side tabulated through
+// value_list; bit 2 = set_output_flag(true) on the first cell (its basis
+// functions as VTU in the working directory).
 int msfem_host_ms_run(int dim, int n_refine, int n_refine_local, int coef, const double *params,
                       double f_value, int bc, int precision, int device, double *u_out, double *M_out,
-                      double *F_out, double *fine_out, int write_vtu) {
+                      double *F_out, double *fine_out, int write_vtu, int options) {
   try {
     if (dim == 2)
       return run_ms<2>(n_refine, n_refine_local, coef, params, f_value, bc, precision, device, u_out,
-                       M_out, F_out, fine_out, write_vtu);
+                       M_out, F_out, fine_out, write_vtu, options);
     if (dim == 3)
       return run_ms<3>(n_refine, n_refine_local, coef, params, f_value, bc, precision, device, u_out,
-                       M_out, F_out, fine_out, write_vtu);
+                       M_out, F_out, fine_out, write_vtu, options);
     g_err = "dim must be 2 or 3";
     return -1;
   } catch (const std::exception &e) {

@@ -175,6 +175,38 @@ def spheres_cube(K=16, seed=4, sphere_seed=44, sizes=(8, 16, 24), contrast=1e4, 
     return problem(3, unit_cube_corners(3, K), nf, coef, f_value=1.0)
 
 
+def gauss_points(prob):
+    """Physical QGauss(2) points of every fine cell, per coarse cell an array
+    [2^d, N_c^d, d] in the TABULATED order (q x fastest over the reference
+    directions, fine cells lexicographic), through the cell's multilinear map."""
+    dim = prob["dim"]
+    nv = 1 << dim
+    g = np.array([0.5 - 0.5 / math.sqrt(3.0), 0.5 + 0.5 / math.sqrt(3.0)])
+    out = []
+    for c in range(prob["corners"].shape[0]):
+        N = int(prob["n_fine_per_cell"][c]) if "n_fine_per_cell" in prob else int(prob["n_fine"])
+        cidx = np.indices((N,) * dim).reshape(dim, -1)[::-1].T  # fine cells, x fastest
+        pts = np.zeros((nv, cidx.shape[0], dim))
+        for q in range(nv):
+            t = (cidx + np.array([g[(q >> a) & 1] for a in range(dim)])) / N
+            for v in range(nv):
+                w = np.ones(t.shape[0])
+                for a in range(dim):
+                    w = w * (t[:, a] if (v >> a) & 1 else 1.0 - t[:, a])
+                pts[q] += w[:, None] * prob["corners"][c, v][None, :]
+        out.append(pts)
+    return out
+
+
+def with_rhs(prob, f):
+    """The problem with a right-hand side f(x) (x [..., d] -> [...]) tabulated
+    at the Gauss points: packed cell blocks [q][fine cell] in "f_qp_values"
+    (RightHandSide::value_list at the QGauss(2) points)."""
+    q = dict(prob)
+    q["f_qp_values"] = np.ascontiguousarray(np.concatenate([f(p).ravel() for p in gauss_points(prob)]))
+    return q
+
+
 def subset(prob, cells):
     """Problem restricted to the given coarse cells (same coefficient)."""
     cells = np.asarray(cells)
@@ -183,6 +215,6 @@ def subset(prob, cells):
     if "n_fine_per_cell" in prob:
         q["n_fine_per_cell"] = np.ascontiguousarray(prob["n_fine_per_cell"][cells])
     q["coef"] = dict(prob["coef"])
-    if prob["coef"].get("kind") == _abi.COEF_TABULATED:
+    if prob["coef"].get("kind") == _abi.COEF_TABULATED or prob.get("f_qp_values") is not None:
         raise ValueError("subset of a tabulated problem: tabulate after subsetting")
     return q

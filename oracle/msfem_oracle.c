@@ -430,6 +430,13 @@ int oc_assemble_cell(const oc_batch *b, int32_t cell, double *st, double *bl) {
   double g[2];
   qgauss2(g);
   const double w = 1.0 / nv; /* QGauss(2) weight per point on [0,1]^d */
+  const double *fq_cell = NULL;
+  if (b->f_qp_values) {
+    int64_t off = 0;
+    if (b->f_qp_offset) off = b->f_qp_offset[cell];
+    else for (int c = 0; c < cell; ++c) off += (int64_t)nv * ipow(cell_n(b, c), dim);
+    fq_cell = b->f_qp_values + off;
+  }
   for (int fc = 0; fc < nfc; ++fc) {
     int cidx[MAXD] = {fc % N, (fc / N) % N, dim == 3 ? fc / (N * N) : 0};
     double V[8 * MAXD];
@@ -449,6 +456,8 @@ int oc_assemble_cell(const oc_batch *b, int32_t cell, double *st, double *bl) {
       double JxW = w * fabs(det);
       double A[9];
       oc_coef_eval(b, cell, fc, q, xq, A);
+      /* f at this Gauss point: RightHandSide::value_list (right_hand_side.tpp:27-40) */
+      const double fq_val = fq_cell ? fq_cell[(size_t)q * nfc + fc] : b->f_value;
       /* physical gradients J^{-T} grad_ref */
       double G[8 * MAXD];
       for (int k = 0; k < nv; ++k)
@@ -469,7 +478,7 @@ int oc_assemble_cell(const oc_batch *b, int32_t cell, double *st, double *bl) {
           for (int a = 0; a < dim; ++a) s += G[j * dim + a] * AG[a];
           K[j * nv + i] += s * JxW; /* A symmetric: grad_j . A grad_i */
         }
-        be[i] += psi[i] * b->f_value * JxW;
+        be[i] += psi[i] * fq_val * JxW;
       }
     }
     for (int i = 0; i < nv; ++i) {

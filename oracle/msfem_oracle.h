@@ -77,6 +77,11 @@ typedef struct oc_batch {
   int32_t ordering;
   int32_t nthreads;
   int32_t raw_monomials;  /* 1: BasisQ1 from untranslated monomials exactly as basis_q1.tpp */
+  /* optional right-hand side at the Gauss points (RightHandSide::value_list,
+   * diffusion_problem_basis.tpp:204-205): per cell 2^d N^d values [q][fine
+   * cell]; f_qp_offset NULL = packed blocks in cell order; NULL = f_value */
+  const double *f_qp_values;
+  const int64_t *f_qp_offset;
 } oc_batch;
 
 /* Whole batch.  M [n][2^d][2^d], F [n][2^d]; optional (may be NULL):

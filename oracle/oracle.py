@@ -56,6 +56,8 @@ class OcBatch(ctypes.Structure):
         ("ordering", ctypes.c_int32),
         ("nthreads", ctypes.c_int32),
         ("raw_monomials", ctypes.c_int32),
+        ("f_qp_values", ctypes.c_void_p),
+        ("f_qp_offset", ctypes.c_void_p),
     ]
 
 
@@ -145,6 +147,18 @@ def make_batch(problem, solver=SOLVER_DIRECT, tol=1e-12, tol_absolute=False, max
             if key == "spheres":
                 b.coef.n_spheres = arr.shape[0]
     b.f_value = float(problem.get("f_value", 1.0))
+    fprob = problem
+    if problem.get("f_qp_values") is not None and problem.get("f_qp_offset") is None:
+        # packed cell blocks of 2^d N_c^d values: explicit offsets
+        nfc = (np.asarray(problem["n_fine_per_cell"], dtype=np.int64) if "n_fine_per_cell" in problem
+               else np.full(b.n_cells, b.n_fine, dtype=np.int64)) ** b.dim
+        fprob = dict(problem)
+        fprob["f_qp_offset"] = np.concatenate([[0], np.cumsum((1 << b.dim) * nfc)[:-1]]).astype(np.int64)
+    for key in ("f_qp_values", "f_qp_offset"):
+        if fprob.get(key) is not None:
+            arr = np.ascontiguousarray(fprob[key], dtype=np.int64 if key == "f_qp_offset" else np.float64)
+            keep.append(arr)
+            setattr(b, key, _p(arr))
     b.tol = float(tol)
     b.tol_absolute = int(bool(tol_absolute))
     b.maxit = int(maxit)

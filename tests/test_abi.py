@@ -40,7 +40,8 @@ def test_struct_layout_matches_c(built, tmp_path):
     """Compile a probe against the header and compare sizeof/offsetof."""
     abi = built._abi
     probe = tmp_path / "probe.c"
-    fields = {"msfem_batch_desc": (abi.BatchDesc, ["coef", "f_value", "tol", "maxit", "warm_basis"]),
+    fields = {"msfem_batch_desc": (abi.BatchDesc, ["coef", "f_value", "tol", "maxit", "warm_basis",
+                                                   "tol_absolute", "f_qp_values", "f_qp_offset"]),
               "msfem_coef_desc": (abi.CoefDesc, ["params", "qp_values", "n_modes", "spheres"]),
               "msfem_stats": (abi.Stats, ["max_rel_residual", "kernel_launches", "d2h_bytes"])}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "msfem_gpu.h"', "int main(void){"]

@@ -15,14 +15,17 @@ def host_lib(pkg):
     vp = ctypes.c_void_p
     lib.msfem_host_ms_run.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp,
                                       ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
-                                      vp, vp, vp, vp, ctypes.c_int]
+                                      vp, vp, vp, vp, ctypes.c_int, ctypes.c_int]
     lib.msfem_host_ms_run.restype = ctypes.c_int
     lib.msfem_host_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     return lib
 
 
+OPT_RELATIVE_TOL, OPT_LINEAR_RHS, OPT_OUTPUT_BASIS = 1, 2, 4
+
+
 def run_host(lib, dim, n_refine, n_refine_local, coef=0, params=(0.0,) * 8, f=2.0, bc=0, precision=0,
-             write_vtu=0):
+             write_vtu=0, options=0):
     K = 1 << n_refine
     N = 1 << n_refine_local
     nv = 1 << dim
@@ -34,7 +37,7 @@ def run_host(lib, dim, n_refine, n_refine_local, coef=0, params=(0.0,) * 8, f=2.
     pr = np.ascontiguousarray(params, dtype=np.float64)
     p = lambda a: ctypes.c_void_p(a.ctypes.data)
     rc = lib.msfem_host_ms_run(dim, n_refine, n_refine_local, coef, p(pr), f, bc, precision, 0,
-                               p(u), p(M), p(F), p(fine), write_vtu)
+                               p(u), p(M), p(F), p(fine), write_vtu, options)
     buf = ctypes.create_string_buffer(512)
     lib.msfem_host_last_error(buf, 512)
     return rc, buf.value.decode(), u, M, F, fine
@@ -107,3 +110,44 @@ def test_reference_driver_3d(pkg, oracle):
     assert np.abs(M - ref["M"]).max() < 1e-10 * np.abs(ref["M"]).max()
     u_ref = oracle.coarse_solve(3, 2, ref["M"], ref["F"], 0)
     assert np.abs(u - u_ref).max() < 1e-10 * max(1.0, np.abs(u_ref).max())
+
+
+@pytest.mark.gpu
+def test_output_flag_writes_basis_vtu(pkg, oracle, tmp_path, monkeypatch):
+    """set_output_flag(true) writes the cell's basis functions as the
+    reference's output_basis does (diffusion_problem_basis.tpp:392-418):
+    "2d-basis.<subdomain>.cell-<id>.vtu" with point data basis_0 .. basis_3."""
+    monkeypatch.chdir(tmp_path)
+    lib = host_lib(pkg)
+    rc, msg, *_ = run_host(lib, 2, 2, 3, options=OPT_OUTPUT_BASIS)
+    assert rc == 0, msg
+    files = sorted(p.name for p in tmp_path.glob("2d-basis.*.vtu"))
+    assert files == ["2d-basis.4294967295.cell-0_0:.vtu"], files
+    text = (tmp_path / files[0]).read_text()
+    ref = oracle.run(pkg.workloads.reference_problem(2, 2, 3), want_basis=True)
+    nodes = 9 * 9
+    basis0 = ref["basis"].reshape(16, 4, nodes)[0]
+    for i in range(4):
+        head = f'Name="basis_{i}" format="ascii">'
+        assert head in text
+        vals = np.array(text.split(head, 1)[1].split("</DataArray>", 1)[0].split(), dtype=float)
+        assert vals.shape == (nodes,)
+        assert np.abs(vals - basis0[i]).max() < 1e-10
+
+
+@pytest.mark.gpu
+def test_right_hand_side_function_and_tolerance_modes(pkg, oracle):
+    """A RightHandSide without a constant value (f = 2 + x) goes through
+    value_list at the Gauss points; both stopping rules (the reference's
+    absolute 1e-12, and relative 1e-12) give the oracle's coarse solution."""
+    lib = host_lib(pkg)
+    W = pkg.workloads
+    prob = W.with_rhs(W.reference_problem(2, 3, 4), lambda x: 2.0 + x[..., 0])
+    ref = oracle.run(prob)
+    u_ref = oracle.coarse_solve(2, 8, ref["M"], ref["F"], 0)
+    for opts in (OPT_LINEAR_RHS, OPT_LINEAR_RHS | OPT_RELATIVE_TOL):
+        rc, msg, u, M, F, _ = run_host(lib, 2, 3, 4, options=opts)
+        assert rc == 0, msg
+        assert np.abs(F - ref["F"]).max() < 1e-10 * np.abs(ref["F"]).max()
+        assert np.abs(M - ref["M"]).max() < 1e-10 * np.abs(ref["M"]).max()
+        assert np.abs(u - u_ref).max() < 1e-10 * np.abs(u_ref).max()

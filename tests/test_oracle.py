@@ -201,3 +201,34 @@ def test_coarse_solve_homogeneous_and_reference(pkg, oracle):
     dbc = ((Xg - 0.5) ** 2 + (Yg - 0.5) ** 2).ravel()
     on_dir = ((Xg == 0) | (Yg == 0)).ravel()
     assert np.abs(u0[on_dir] - dbc[on_dir]).max() < 1e-15
+
+
+def test_tabulated_rhs_constant_equals_f_value(pkg, oracle):
+    """f tabulated at the Gauss points (RightHandSide::value_list) with a
+    constant value gives the constant-f load, on a bilinear cell too."""
+    W = pkg.workloads
+    corners = W.unit_cube_corners(2, 2).copy()
+    corners[3, 3] += [0.05, -0.03]  # a general (non-parallelogram) cell
+    prob = W.problem(2, corners, 6, {"kind": 2, "params": [0.5, 0.25]}, f_value=2.0)
+    tab = W.with_rhs(prob, lambda x: np.full(x.shape[:-1], 2.0))
+    a = oracle.run(prob)
+    b = oracle.run(tab)
+    assert np.abs(a["F"] - b["F"]).max() <= 1e-15 * np.abs(a["F"]).max() * 10
+    assert np.array_equal(a["M"], b["M"])
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_tabulated_rhs_integrates_linear_f_exactly(pkg, oracle, dim):
+    """sum_i F_i = int_K f (the basis is a partition of unity and QGauss(2)
+    integrates a linear f exactly on affine cells), on uneven N."""
+    W = pkg.workloads
+    K = 2
+    corners = W.unit_cube_corners(dim, K)
+    nf = np.array([3, 4, 2, 5, 4, 3, 2, 3][:K ** dim], dtype=np.int32)
+    prob = W.problem(dim, corners, nf, {"kind": 2, "params": [0.7, 0.5]})
+    w = np.array([1.0, 2.0, 3.0][:dim])
+    prob = W.with_rhs(prob, lambda x: 1.0 + x @ w)
+    r = oracle.run(prob, tol=1e-13)
+    centers = corners.mean(axis=1)
+    exact = (1.0 / K) ** dim * (1.0 + centers @ w)
+    assert np.abs(r["F"].sum(axis=1) - exact).max() < 1e-12

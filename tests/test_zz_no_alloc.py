@@ -110,18 +110,27 @@ def test_noalloc_allocates_nothing(pkg, engine):
     assert np.all(out[2].cpu().numpy() == abi.CELL_CONVERGED)
 
 
-def test_noalloc_tabulated_coefficient(pkg, engine):
-    """Device-resident tabulated random-Fourier tensor, N = 32."""
+@pytest.mark.parametrize("reference_stop", [False, True])
+def test_noalloc_tabulated_coefficient(pkg, engine, reference_stop):
+    """Device-resident tabulated random-Fourier tensor, N = 32; with
+    reference_stop, also f tabulated at the Gauss points and the absolute
+    residual stop of the reference's SolverControl."""
     torch = pytest.importorskip("torch")
     abi = pkg._abi
     lib = abi.load()
     W = pkg.workloads
     prob = W.subset(W.fourier_square(K=64, N=32), [0, 17, 300, 1999, 4095])
     tab = engine.tabulate(prob, 3)
-    ref = engine.run(prob, precision="fp64", tol=1e-11, want_basis=True)
+    if reference_stop:
+        prob = W.with_rhs(prob, lambda x: 2.0 + x[..., 0] * x[..., 1])
+    ref = engine.run(prob, precision="fp64", tol=1e-11, want_basis=True, tol_absolute=reference_stop)
     corners_d = torch.from_numpy(prob["corners"]).cuda()
     qp_d = torch.from_numpy(tab).cuda()
     d = device_desc(abi, prob, corners_d, abi.PREC_FP64, 1e-11, qp_d=qp_d, ncomp=3)
+    if reference_stop:
+        fq_d = torch.from_numpy(prob["f_qp_values"]).cuda()
+        d.f_qp_values = fq_d.data_ptr()
+        d.tol_absolute = 1
     for _ in range(2):
         M, F, B, st = run_noalloc(torch, lib, abi, d, 5, 33 * 33)
         assert np.all(st == abi.CELL_CONVERGED)
