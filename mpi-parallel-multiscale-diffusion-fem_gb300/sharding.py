@@ -30,6 +30,35 @@ def block_partition(n_cells, world, rank):
     return start, start + base + (1 if rank < extra else 0)
 
 
+def assemble_blocks(blocks, n_cells):
+    """Per-cell arrays of a strongly sharded batch from every rank's block:
+    blocks = [(start, stop, [array, ...]), ...] (arrays with leading dimension
+    stop - start).  Every cell must be owned by exactly one block."""
+    owner = np.zeros(int(n_cells), dtype=np.int64)
+    out = None
+    for start, stop, arrays in blocks:
+        owner[start:stop] += 1
+        if out is None:
+            out = [np.zeros((int(n_cells),) + np.asarray(a).shape[1:], dtype=np.asarray(a).dtype) for a in arrays]
+        for o, a in zip(out, arrays):
+            o[start:stop] = a
+    if not np.all(owner == 1):
+        raise ValueError("cells owned by no rank or by several: "
+                         f"{np.flatnonzero(owner != 1)[:8].tolist()}")
+    return out
+
+
+def gather_blocks(arrays, start, stop, n_cells, dist=None):
+    """Outputs of a strongly sharded batch on every rank (the host-side
+    all-gather of each rank's [start, stop) block; the basis computation
+    itself exchanges nothing).  Identity at one rank."""
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return assemble_blocks([(start, stop, arrays)], n_cells)
+    blocks = [None] * dist.get_world_size()
+    dist.all_gather_object(blocks, (int(start), int(stop), [np.asarray(a) for a in arrays]))
+    return assemble_blocks(blocks, n_cells)
+
+
 def max_over_ranks(value, dist=None, device="cpu"):
     """Job time = the slowest rank's time (a MAX all-reduce; identity at 1 rank)."""
     if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
