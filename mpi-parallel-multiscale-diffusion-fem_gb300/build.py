@@ -4,6 +4,8 @@
   lib/libmsfem_host.so  C++ host layer mirroring the reference's
                         DiffusionProblemBasis / coefficient interfaces,
                         linked against libmsfem_gpu.so
+  lib/libmsfem_fields.so  host generators of the synthetic coefficient
+                        fields (no CUDA)
 """
 import os
 import subprocess
@@ -120,5 +122,20 @@ def build_host(force=False, quiet=True):
     return target
 
 
+def build_fields(force=False, quiet=True):
+    """Field generators; no fused multiply-adds, so the results are the same
+    bits on every host (and as the Python restatement in the tests)."""
+    src = os.path.join(HOST, "fields.cpp")
+    os.makedirs(LIB_DIR, exist_ok=True)
+    target = os.path.join(LIB_DIR, "libmsfem_fields.so")
+    if force or _stale(target, [src, os.path.join(INCLUDE, "msfem_fields.h")]):
+        cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-I", INCLUDE,
+               "-o", target + ".tmp", src]
+        _run(cmd, quiet)
+        os.replace(target + ".tmp", target)
+    return target
+
+
 def build_all(force=False, quiet=True):
-    return [build_gpu(force, quiet), build_probe(force, quiet), build_host(force, quiet)]
+    return [build_gpu(force, quiet), build_probe(force, quiet), build_host(force, quiet),
+            build_fields(force, quiet)]

@@ -81,44 +81,47 @@ def fourier_coef(seeds, dim=2, n_modes=64, kmax=128 * math.pi, variance=1.0 / 64
             "n_modes": n_modes}
 
 
+_fields_lib = None
+
+
+def _fields():
+    """libmsfem_fields.so (built by build.build_fields)."""
+    global _fields_lib
+    if _fields_lib is None:
+        import ctypes
+        import os
+
+        path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib", "libmsfem_fields.so")
+        if not os.path.exists(path):
+            raise OSError(f"libmsfem_fields.so not found at {path}: run build() first")
+        lib = ctypes.CDLL(path)
+        lib.msfem_spheres_rsa.argtypes = [ctypes.c_uint64, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                          ctypes.c_int32, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
+                                          ctypes.POINTER(ctypes.c_int64)]
+        lib.msfem_spheres_rsa.restype = ctypes.c_int
+        _fields_lib = lib
+    return _fields_lib
+
+
 def spheres_rsa(seed, rmin=0.004, rmax=0.012, fraction=0.2, dim=3, max_tries=10_000_000):
     """Random sequential addition of non-overlapping spheres (discs in 2D) with
     radius U[rmin, rmax], centres U[0,1]^d, until the summed volume reaches
-    `fraction` of the unit cube.  Returns [n, 4] (cx, cy, cz, r)."""
-    rng = SplitMix64(seed)
-    h = 2 * rmax
-    G = int(math.ceil(1.0 / h))
-    grid = {}
-    out = []
-    vol = 0.0
-    unit = (4.0 / 3.0) * math.pi if dim == 3 else math.pi
-    tries = 0
-    while vol < fraction and tries < max_tries:
-        tries += 1
-        r = rmin + (rmax - rmin) * rng.uniform()
-        c = [rng.uniform() for _ in range(dim)]
-        gi = [min(G - 1, int(c[a] / h)) for a in range(dim)]
-        ok = True
-        rng_ = range(-1, 2)
-        if dim == 3:
-            neigh = [(gi[0] + i, gi[1] + j, gi[2] + k) for i in rng_ for j in rng_ for k in rng_]
-        else:
-            neigh = [(gi[0] + i, gi[1] + j) for i in rng_ for j in rng_]
-        for key in neigh:
-            for s in grid.get(key, ()):
-                d2 = sum((c[a] - s[a]) ** 2 for a in range(dim))
-                if d2 < (r + s[3]) ** 2:
-                    ok = False
-                    break
-            if not ok:
-                break
-        if not ok:
-            continue
-        sph = (c[0], c[1], c[2] if dim == 3 else 0.0, r)
-        grid.setdefault(tuple(gi), []).append(sph)
-        out.append(sph)
-        vol += unit * r ** dim
-    return np.array(out, dtype=np.float64).reshape(-1, 4)
+    `fraction` of the unit cube (msfem_spheres_rsa of libmsfem_fields.so).
+    Returns [n, 4] (cx, cy, cz, r)."""
+    import ctypes
+
+    lib = _fields()
+    n = ctypes.c_int64(0)
+    cap = 1 << 16
+    while True:
+        out = np.zeros((cap, 4))
+        rc = lib.msfem_spheres_rsa(seed, rmin, rmax, fraction, dim, max_tries, out.ctypes.data, cap,
+                                   ctypes.byref(n))
+        if rc == 0:
+            return np.ascontiguousarray(out[:n.value])
+        if rc != 1:
+            raise ValueError("msfem_spheres_rsa: bad arguments")
+        cap = int(n.value)
 
 
 def problem(dim, corners, n_fine, coef, f_value=1.0):
