@@ -259,9 +259,12 @@ def main():
     def max_over_ranks(x):
         return pkg.sharding.max_over_ranks(x, torch.distributed if world > 1 else None, f"cuda:{local}")
 
+    tab_times = {}
+
     def make_ws(prob, shift):
         """Device workload: corners + the coefficient tabulated at the Gauss
-        points (input data, tabulated once by the library's field kernel)."""
+        points (input data, tabulated once by the library's field kernel;
+        the tabulation's device time is kept in tab_times by cell count)."""
         corners_h = pkg.sharding.weak_shard_corners(prob["corners"], shift)
         n = corners_h.shape[0]
         corners_d = torch.from_numpy(corners_h).to(f"cuda:{local}")
@@ -276,9 +279,15 @@ def main():
         dt.tol, dt.maxit = TOL, 1000
         size = eng.lib.msfem_tabulated_size(ctypes.byref(dt), 3)
         tab_d = torch.empty(size, dtype=torch.float64, device=f"cuda:{local}")
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
         rc = eng.lib.msfem_tabulate_coefficient(eng.handle, ctypes.byref(dt), 3, tab_d.data_ptr())
+        ev1.record(stream)
         if rc != abi.OK:
             raise abi.MsfemError(rc, abi.last_error(eng.lib))
+        torch.cuda.synchronize()
+        tab_times[n] = {"ms": ev0.elapsed_time(ev1), "bytes": int(size * 8)}
         ws = {"n": n, "corners_h": corners_h, "corners_d": corners_d, "tab_d": tab_d, "size": size,
               "M": torch.empty((n, 4, 4), dtype=torch.float64, device=f"cuda:{local}"),
               "F": torch.empty((n, 4), dtype=torch.float64, device=f"cuda:{local}"),
@@ -569,6 +578,14 @@ def main():
             "speedup_mixed_vs_fp64": ms3f / ms3m,
         }
         line["gpu_launches_fourier_256x256"] = st3 + 2
+        # field generation: the random-Fourier tensor tabulated at the Gauss
+        # points on the device (phase recurrence along lattice rows)
+        tt = tab_times.get(ws3["n"])
+        if tt:
+            line["fourier_256x256"]["tabulation"] = {
+                "ms": tt["ms"], "bytes_written": tt["bytes"],
+                "hbm_frac_of_measured": tt["bytes"] / (tt["ms"] * 1e-3) / 1e9 / read_peaks()[0].get("hbm_gbs", 1),
+                "note": "3 fields x 64 modes per Gauss point in FP64; bound by the FP64 pipe, not HBM"}
         # per-basis energy-norm and coarse-matrix errors of every cell against
         # the FP64 form solved to 1e-12 (untimed)
         ref3 = solve_with_basis(ws3, abi.PREC_FP64, 1e-12)
@@ -736,10 +753,31 @@ def main():
                 del got
             sur.detach()
             del ref3
+        # cost of the prediction itself, timed apart: node features and the
+        # network's forward pass over all 65536 cells (the warm-started solve
+        # also composes Q1 + delta and evaluates the FP64 initial residual)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e2 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        f5 = S.features(eng, desc5, torch)
+        e1.record(stream)
+        p5 = torch.empty((desc5.n_cells, 4, 33, 33), dtype=torch.float32, device=f"cuda:{local}")
+        sur.predict(f5, p5)
+        e2.record(stream)
+        torch.cuda.synchronize()
+        infer = {"features_ms": e0.elapsed_time(e1), "network_ms": e1.elapsed_time(e2)}
+        del f5, p5
         for pname in ("mixed", "fp64"):
             c, w = ev[f"{pname}_cold"], ev[f"{pname}_surrogate"]
             w["iterations_saved"] = 1.0 - w["mean_iterations"] / c["mean_iterations"]
             w["speedup_vs_cold"] = c["ms"] / w["ms"]
+            # what the fewer iterations save, against what the prediction costs
+            w["breakdown_ms"] = {"cold_solve": c["ms"], "warm_total": w["ms"], **infer,
+                                 "warm_without_prediction": w["ms"] - infer["features_ms"] - infer["network_ms"],
+                                 "saved_by_fewer_iterations": c["ms"] - (w["ms"] - infer["features_ms"]
+                                                                         - infer["network_ms"])}
         ev["mixed_surrogate"]["speedup_vs_fp64_cold"] = ev["fp64_cold"]["ms"] / ev["mixed_surrogate"]["ms"]
         line["surrogate"] = {
             "network": "6 conv3x3 layers 3-32-32-32-32-32-4, dilations 1/2/4/8/2/1, BF16 weights and "

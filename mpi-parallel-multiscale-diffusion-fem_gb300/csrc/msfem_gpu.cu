@@ -143,7 +143,115 @@ __device__ bool inside_sphere(const TabParams &t, const double *x) {
   return false;
 }
 
+// Random-Fourier fields on an affine cell.  Along a lattice row of Gauss
+// points (fixed y[, z] and Gauss-point offsets, x advancing by one fine cell)
+// the point moves by the constant vector e1 = (v1 - v0) / N, so every mode's
+// phase advances by the constant k . e1: cos and sin of the phase follow the
+// angle-addition recurrence (one 2 x 2 rotation per point) instead of one cos
+// per point and mode.  Each segment of kSeg points starts from a direct
+// sincos of its first phase, which bounds the recurrence's rounding drift to
+// kSeg steps (a few 1e-15 relative).  Pass 1: one task per (field, row,
+// segment) sums its field along the segment into the output block (as
+// scratch, component f = field f).  Pass 2 (2D): each point's three fields
+// become the tensor components in place.
+constexpr int kSeg = 16;
+
+__device__ void tabulate_fourier_affine(const TabParams &t, const double *cr, int N, int nfc, double *out,
+                                        double *rot /* [fields][n_modes][2] shared */) {
+  const int dim = t.dim, nv = 1 << dim;
+  const int nf = dim == 2 ? 3 : 1;
+  const double invN = 1.0 / N;
+  double e[3][3];  // e[a] = (v_{2^a} - v0) / N
+  for (int a = 0; a < dim; ++a)
+    for (int b = 0; b < dim; ++b) e[a][b] = (cr[(1 << a) * dim + b] - cr[b]) * invN;
+  // cos / sin of each mode's phase step along x
+  for (int i = threadIdx.x; i < nf * t.n_modes; i += blockDim.x) {
+    const double *md = t.modes + (int64_t)i * 5;
+    const double dph = md[0] * e[0][0] + md[1] * e[0][1] + (dim == 3 ? md[2] * e[0][2] : 0.0);
+    sincos(dph, &rot[2 * i + 1], &rot[2 * i]);
+  }
+  __syncthreads();
+  const int nseg = (N + kSeg - 1) / kSeg;
+  const int rows = (dim == 2 ? N : N * N) * nv;  // (y[, z], Gauss-point offsets)
+  const int tasks = nf * rows * nseg;
+  for (int task = threadIdx.x; task < tasks; task += blockDim.x) {
+    const int seg = task % nseg, row = (task / nseg) % rows, f = task / (nseg * rows);
+    const int q = row % nv, yz = row / nv;
+    const int cy = yz % N, cz = dim == 3 ? yz / N : 0;
+    const int cx0 = seg * kSeg;
+    const double u[3] = {cx0 + gauss2(q & 1), cy + gauss2((q >> 1) & 1), cz + gauss2((q >> 2) & 1)};
+    double x0[3];
+    for (int b = 0; b < dim; ++b) {
+      x0[b] = cr[b];
+      for (int a = 0; a < dim; ++a) x0[b] = fma(e[a][b], u[a], x0[b]);
+    }
+    double g[kSeg];
+#pragma unroll
+    for (int j = 0; j < kSeg; ++j) g[j] = 0.0;
+    const double *md = t.modes + (int64_t)f * t.n_modes * 5;
+    const double *rf = rot + 2 * f * t.n_modes;
+    for (int m = 0; m < t.n_modes; ++m) {
+      const double ph = md[5 * m] * x0[0] + md[5 * m + 1] * x0[1] + (dim == 3 ? md[5 * m + 2] * x0[2] : 0.0) +
+                        md[5 * m + 4];
+      double c, sn;
+      sincos(ph, &sn, &c);
+      const double amp = md[5 * m + 3], cd = rf[2 * m], sd = rf[2 * m + 1];
+#pragma unroll
+      for (int j = 0; j < kSeg; ++j) {
+        g[j] = fma(amp, c, g[j]);
+        const double c2 = c * cd - sn * sd;
+        sn = fma(sn, cd, c * sd);
+        c = c2;
+      }
+    }
+    const int fc0 = (cz * N + cy) * N + cx0;
+    const int cnt = min(kSeg, N - cx0);
+    if (dim == 2) {
+      double *o = out + ((int64_t)f * nv + q) * nfc + fc0;
+#pragma unroll
+      for (int j = 0; j < kSeg; ++j)
+        if (j < cnt) o[j] = g[j];
+    } else {
+      // 3D: a = exp(g1); ncomp 6 writes the diagonal tensor a I
+#pragma unroll
+      for (int j = 0; j < kSeg; ++j)
+        if (j < cnt) {
+          const double a = exp(g[j]);
+          if (t.ncomp == 1) {
+            out[(int64_t)q * nfc + fc0 + j] = a;
+          } else {
+            const double comp[6] = {a, 0.0, 0.0, a, 0.0, a};
+            for (int k = 0; k < 6; ++k) out[((int64_t)k * nv + q) * nfc + fc0 + j] = comp[k];
+          }
+        }
+    }
+  }
+  if (dim == 3) return;
+  __syncthreads();
+  // 2D: A = R(theta) diag(e^g1, e^g2) R(theta)^T from the three fields, in place
+  for (int i = threadIdx.x; i < nv * nfc; i += blockDim.x) {
+    const double g1 = out[i], g2 = out[(int64_t)nv * nfc + i], th = out[2 * (int64_t)nv * nfc + i];
+    double sn, cn;
+    sincos(th, &sn, &cn);
+    const double e1 = exp(g1), e2 = exp(g2);
+    out[i] = cn * cn * e1 + sn * sn * e2;
+    out[(int64_t)nv * nfc + i] = cn * sn * (e1 - e2);
+    out[2 * (int64_t)nv * nfc + i] = sn * sn * e1 + cn * cn * e2;
+  }
+}
+
+__device__ __forceinline__ bool affine_corners(const double *cr, int dim) {
+  for (int k = 0; k < (1 << dim); ++k)
+    for (int a = 0; a < dim; ++a) {
+      const double pred = cr[a] + ((k & 1) ? cr[dim + a] - cr[a] : 0.0) +
+                          ((k & 2) ? cr[2 * dim + a] - cr[a] : 0.0) + ((k & 4) ? cr[4 * dim + a] - cr[a] : 0.0);
+      if (pred != cr[k * dim + a]) return false;
+    }
+  return true;
+}
+
 __global__ void tabulate_kernel(const TabParams t) {
+  extern __shared__ double tab_rot[];
   const int cell = blockIdx.x;
   if (cell >= t.n_cells) return;
   const int dim = t.dim, nv = 1 << dim;
@@ -152,6 +260,10 @@ __global__ void tabulate_kernel(const TabParams t) {
   if (dim == 3) nfc *= N;
   const double *cr = t.corners + (int64_t)cell * nv * dim;
   double *out = t.out + (t.offset ? t.offset[cell] : (int64_t)cell * t.ncomp * nv * nfc);
+  if (t.kind == MSFEM_COEF_FOURIER && (dim == 3 || t.ncomp == 3) && affine_corners(cr, dim)) {
+    tabulate_fourier_affine(t, cr, N, nfc, out, tab_rot);
+    return;
+  }
   const double invN = 1.0 / N;
   for (int fc = threadIdx.x; fc < nfc; fc += blockDim.x) {
     const int cx = fc % N, cy = (fc / N) % N, cz = dim == 3 ? fc / (N * N) : 0;
@@ -476,7 +588,13 @@ int run_tabulate(msfem_handle *h, const msfem_batch_desc *d, const std::vector<i
     t.sg_h = hh;
   }
   if (d->n_cells == 0) return MSFEM_OK;
-  msfem::tabulate_kernel<<<d->n_cells, 256, 0, h->stream>>>(t);
+  // shared memory: the per-mode phase-step rotations of the FOURIER kind
+  const size_t rot_bytes =
+      t.kind == MSFEM_COEF_FOURIER ? sizeof(double) * 2 * (d->dim == 2 ? 3 : 1) * (size_t)t.n_modes : 0;
+  if (rot_bytes > 48 * 1024)
+    MSFEM_CUDA(cudaFuncSetAttribute(msfem::tabulate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)rot_bytes));
+  msfem::tabulate_kernel<<<d->n_cells, 256, rot_bytes, h->stream>>>(t);
   MSFEM_CUDA(cudaGetLastError());
   (*launches)++;
   (void)nf;

@@ -67,10 +67,28 @@ def test_random_fourier_tensor_parity(pkg, oracle, engine, precision):
 
 
 def test_tabulation_matches_oracle(pkg, oracle, engine):
+    """The field generator against the oracle's direct evaluation: affine
+    cells take the phase-recurrence path, a bilinear cell the per-point one."""
     W = pkg.workloads
-    prob = W.subset(W.fourier_square(K=64, N=32), [5, 700])
+    prob = W.subset(W.fourier_square(K=64, N=32), [5, 700, 4095])
+    corners = prob["corners"].copy()
+    corners[2, 3] += [-0.0011, 0.0007]  # cell 4095 made bilinear
+    prob["corners"] = corners
     a = engine.tabulate(prob, 3)
     b = oracle.tabulate(prob, 3)
+    assert np.abs(a - b).max() < 1e-12 * np.abs(b).max()
+
+
+@pytest.mark.parametrize("ncomp", [1, 6])
+def test_tabulation_matches_oracle_3d(pkg, oracle, engine, ncomp):
+    """3D log-normal Fourier field (a = exp g1) on uneven N up to 24, both
+    output layouts (scalar, and the tensor a I)."""
+    W = pkg.workloads
+    coef = W.fourier_coef((9,), dim=3, n_modes=48, kmax=64 * np.pi)
+    prob = W.problem(3, W.unit_cube_corners(3, 4)[[0, 21, 63]], np.array([24, 7, 17], dtype=np.int32), coef)
+    a = engine.tabulate(prob, ncomp)
+    b = oracle.tabulate(prob, ncomp)
+    assert a.shape == b.shape
     assert np.abs(a - b).max() < 1e-12 * np.abs(b).max()
 
 
