@@ -95,6 +95,7 @@ struct CellShared3D {
   int inner_iters[8];  // mixed form: inner FP32 iterations per RHS
   float seg_thr[8];    // mixed form: stopping threshold on r.r of the current segment
   float seg_rho[2][8]; // mixed form: r.r of the current and next inner iteration
+  float seg_beta[8];   // mixed form, slab cluster shape: beta of the next inner iteration
   int offs[13];        // grid offsets of the forward couplings
   int status;
   int affine;
@@ -603,6 +604,309 @@ __device__ __noinline__ void inner_segment3d(const float *__restrict__ c32, floa
   }
 }
 
+// ---------------------------------------------------------------------------
+// On-chip inner loop of the cluster shape (mixed form).  The CS CTAs of a
+// cluster split the cell's interior z-planes into contiguous slabs of at most
+// SMAX planes (block partition, empty slabs last).  Each CTA keeps in shared
+// memory
+//   - the inner residual r of its planes plus one halo plane on either side
+//     (RHS 0-3 and 4-7 in two float4 arrays, so a warp's 16-byte loads hit
+//     distinct banks), in planes of fixed row stride kRS and plane stride kPS
+//     whose last column and row stay zero: the cell's zero Dirichlet ring,
+//     reached at compile-time offsets without bounds tests;
+//   - the FP32 couplings of its planes (13 forward ones per interior node,
+//     row stride kMaxM) plus the 9 upward couplings of the plane below;
+//   - RHS 4-7 of the correction d of its nodes.
+// A thread owns one (x, y) column of the slab; its search direction p, A p
+// and RHS 0-3 of d stay in registers.  The CG runs in the form that applies
+// the stencil to r: q = A r + beta q equals A p for p = r + beta p, so one
+// cluster barrier covers both the halo exchange of r and the sum of r.r, and
+// the other the sum of p.q: two cluster barriers per iteration.  Global
+// memory is read once per segment (r, couplings) and written once (d).
+// ---------------------------------------------------------------------------
+template <int SMAX>
+struct Slab3D {
+  static constexpr int kMaxM = kNMax3D - 1;          // interior nodes per direction
+  static constexpr int kRS = kMaxM + 1;              // row stride of the r planes (one zero column)
+  static constexpr int kPS = kRS * (kMaxM + 1);      // plane stride of the r planes (one zero row)
+  static constexpr int kPad = 32;                    // zero entries before the first r plane
+  static constexpr int kMaxCol = kMaxM * kMaxM;      // coupling plane (row stride kMaxM)
+  static constexpr int kCPad = 32;                   // zero couplings before and after
+  static constexpr size_t kV = size_t(kPad + (SMAX + 2) * kPS) * 16;                 // one half of r
+  static constexpr size_t kCpl = size_t(2 * kCPad + (SMAX * 13 + 9) * kMaxCol) * 4;
+  static constexpr size_t kD = size_t(SMAX) * kMaxCol * 16;                          // RHS 4-7 of d
+  static constexpr size_t kPart = 2 * 8 * 4;                                         // cluster-sum partials
+  static constexpr size_t bytes = 2 * kV + kCpl + kD + kPart;
+  static_assert(kV % 16 == 0 && kCpl % 16 == 0 && kD % 16 == 0, "16-byte aligned regions");
+};
+
+// Slab of cluster rank c: planes [lo, lo + S) of the m interior planes.
+__device__ __forceinline__ void slab_range(int m, int CS, int c, int &lo, int &S) {
+  const int base = m / CS, extra = m % CS;
+  lo = 1 + c * base + min(c, extra);
+  S = c < CS ? base + (c < extra ? 1 : 0) : 0;
+}
+
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+
+// One xy-site (DX, DY) of a column's stencil: the r values of the site in
+// every plane of the slab and its halos, applied to every owned node within
+// one plane of it.  A node's coupling with the site is its own forward
+// coupling, or the neighbour's forward coupling back (for the plane below the
+// slab, from the halo coupling block).  At a site on the cell's boundary r is
+// zero, so whatever finite coupling the compile-time offset reads there
+// contributes nothing.
+template <int SMAX, int DX, int DY>
+__device__ __forceinline__ void slab_site(const float4 *__restrict__ rlo, const float4 *__restrict__ rhi,
+                                          const float *__restrict__ cpl, int lpos, int ccol, int S,
+                                          float2 (&q)[SMAX][4]) {
+  using S3 = Slab3D<SMAX>;
+  constexpr int kRoff = DY * S3::kRS + DX, kCoff = DY * S3::kMaxM + DX;
+#pragma unroll
+  for (int zz = 0; zz < SMAX + 2; ++zz) {
+    if (zz >= S + 2) break;
+    const float4 a = rlo[zz * S3::kPS + lpos + kRoff];
+    const float4 b = rhi[zz * S3::kPS + lpos + kRoff];
+#pragma unroll
+    for (int s = 0; s < SMAX; ++s) {
+      const int dz = zz - 1 - s;
+      if (dz < -1 || dz > 1 || s >= S) continue;
+      float c;
+      if (DX == 0 && DY == 0 && dz == 0) {
+        c = 1.0f;  // the scaled operator has a unit diagonal
+      } else if (fwd_dir(DX, DY, dz)) {
+        c = cpl[(s * 13 + fwd_slot(DX, DY, dz)) * S3::kMaxCol + ccol];
+      } else if (dz == 0) {
+        c = cpl[(s * 13 + fwd_slot(-DX, -DY, 0)) * S3::kMaxCol + ccol + kCoff];
+      } else if (s >= 1) {
+        c = cpl[((s - 1) * 13 + fwd_slot(-DX, -DY, 1)) * S3::kMaxCol + ccol + kCoff];
+      } else {
+        c = cpl[(SMAX * 13 + fwd_slot(-DX, -DY, 1) - 4) * S3::kMaxCol + ccol + kCoff];
+      }
+      const float2 cc = f2(c, c);
+      q[s][0] = __ffma2_rn(cc, f2(a.x, a.y), q[s][0]);
+      q[s][1] = __ffma2_rn(cc, f2(a.z, a.w), q[s][1]);
+      q[s][2] = __ffma2_rn(cc, f2(b.x, b.y), q[s][2]);
+      q[s][3] = __ffma2_rn(cc, f2(b.z, b.w), q[s][3]);
+    }
+  }
+}
+
+template <int SMAX, int DY>
+__device__ __forceinline__ void slab_row(const float4 *__restrict__ rlo, const float4 *__restrict__ rhi,
+                                         const float *__restrict__ cpl, int lpos, int ccol, int S,
+                                         float2 (&q)[SMAX][4]) {
+  slab_site<SMAX, -1, DY>(rlo, rhi, cpl, lpos, ccol, S, q);
+  slab_site<SMAX, 0, DY>(rlo, rhi, cpl, lpos, ccol, S, q);
+  slab_site<SMAX, 1, DY>(rlo, rhi, cpl, lpos, ccol, S, q);
+}
+
+// Sum of 8 values over every thread of the cluster, in a fixed order (warp
+// transposes, the CTA's warps in order, then the CTAs in rank order with a
+// commutative butterfly), so every thread of every CTA gets the same bits.
+// Includes the cluster barrier that publishes the shared-memory writes made
+// before the call (the partials, and the halo planes pushed to neighbours).
+template <int NT, int CS>
+__device__ __forceinline__ void cluster_sum8(float (&v)[8], float *redw, float *part, int slot, int lane,
+                                             int warp) {
+  constexpr int NW = NT / 32;
+  float vv[8];
+#pragma unroll
+  for (int r = 0; r < 8; ++r) vv[r] = v[r];
+  const float t = warp_transpose_reduce<8>(vv, lane);
+  if ((lane & 3) == 0) redw[warp * 8 + (lane >> 2)] = t;
+  __syncthreads();
+  if (warp == 0 && lane < 8) {
+    float s = 0.f;
+    for (int w = 0; w < NW; ++w) s += redw[w * 8 + lane];
+    part[slot * 8 + lane] = s;
+  }
+  csync<CS>();
+  float s = 0.f;
+  for (int c = lane >> 3; c < CS; c += 4) s += peer<CS>(part, c)[slot * 8 + (lane & 7)];
+  s += shfl_xor_d(s, 8);
+  s += shfl_xor_d(s, 16);
+#pragma unroll
+  for (int r = 0; r < 8; ++r) v[r] = __shfl_sync(0xffffffffu, s, r);
+}
+
+// One refinement segment of the inner FP32 CG on the slabs (see above).
+// In: rr32 = the FP32 residual on every interior node (node-major), written
+// before the last cluster barrier; cs.seg_rho[0] = r.r, cs.seg_thr the
+// stopping thresholds.  Out: dd32 = the correction on every interior node,
+// visible to the whole cluster on return.
+template <int NT, int CS, int SMAX>
+__device__ __noinline__ void inner_segment3d_slab(const float *__restrict__ c32, const float *__restrict__ rr32,
+                                                  float *__restrict__ dd32, long G, int N, int P, int inner_maxit,
+                                                  unsigned iact, float *redw, CellShared3D &cs,
+                                                  unsigned char *dsm) {
+  using S3 = Slab3D<SMAX>;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int crank = cluster_rank<CS>();
+  const int m = N - 1, mm = m * m;
+  int lo, S, lo_nb, S_dn, S_up;
+  slab_range(m, CS, crank, lo, S);
+  slab_range(m, CS, crank > 0 ? crank - 1 : 0, lo_nb, S_dn);
+  slab_range(m, CS, crank + 1, lo_nb, S_up);
+  float4 *rlo = reinterpret_cast<float4 *>(dsm) + S3::kPad;
+  float4 *rhi = reinterpret_cast<float4 *>(dsm + S3::kV) + S3::kPad;
+  float *cpl = reinterpret_cast<float *>(dsm + 2 * S3::kV) + S3::kCPad;
+  float4 *dhi = reinterpret_cast<float4 *>(dsm + 2 * S3::kV + S3::kCpl);
+  float *part = reinterpret_cast<float *>(dsm + 2 * S3::kV + S3::kCpl + S3::kD);
+  const bool own = tid < mm && S > 0;
+  const int col = own ? tid : 0;
+  const int ix = 1 + col % m, iy = 1 + col / m;
+  const int lpos = (iy - 1) * S3::kRS + (ix - 1);     // position in an r plane
+  const int ccol = (iy - 1) * S3::kMaxM + (ix - 1);   // position in a coupling plane
+  const int rdn = crank > 0 ? crank - 1 : crank, rup = crank + 1 < CS ? crank + 1 : crank;
+  const bool push_dn = own && crank > 0;
+  const bool push_up = own && crank + 1 < CS && S_up > 0;
+
+  // set-up: zero r (halo planes on the cell's boundary, the zero ring) and the
+  // couplings (padding, unused positions), then load this slab's couplings
+  {
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 *v = reinterpret_cast<float4 *>(dsm);
+    for (int i = tid; i < (int)(2 * S3::kV / 16); i += NT) v[i] = z4;
+    float *c = reinterpret_cast<float *>(dsm + 2 * S3::kV);
+    for (int i = tid; i < (int)(S3::kCpl / 4); i += NT) c[i] = 0.f;
+  }
+  __syncthreads();
+  for (int i = tid; i < S * 13 * mm; i += NT) {
+    const int c = i % mm, so = i / mm, o = so % 13, sl = so / 13;
+    const int jx = c % m, jy = c / m;
+    cpl[(sl * 13 + o) * S3::kMaxCol + jy * S3::kMaxM + jx] = c32[o * G + grid3(P, 1 + jx, 1 + jy, lo + sl)];
+  }
+  if (lo - 1 >= 1)
+    for (int i = tid; i < 9 * mm; i += NT) {
+      const int c = i % mm, j = i / mm;
+      const int jx = c % m, jy = c / m;
+      cpl[(SMAX * 13 + j) * S3::kMaxCol + jy * S3::kMaxM + jx] = c32[(4 + j) * G + grid3(P, 1 + jx, 1 + jy, lo - 1)];
+    }
+  csync<CS>();  // every CTA's r is zeroed before any halo is pushed into it
+  // the neighbours' addresses are mapped at each push (few registers live
+  // through the inner loop: the 17-warp shape runs at 96 per thread)
+  auto push_halos = [&]() {
+    if (push_dn) {  // bottom plane -> the top halo of the CTA below
+      peer<CS>(rlo, rdn)[(S_dn + 1) * S3::kPS + lpos] = rlo[S3::kPS + lpos];
+      peer<CS>(rhi, rdn)[(S_dn + 1) * S3::kPS + lpos] = rhi[S3::kPS + lpos];
+    }
+    if (push_up) {  // top plane -> the bottom halo of the CTA above
+      peer<CS>(rlo, rup)[lpos] = rlo[S * S3::kPS + lpos];
+      peer<CS>(rhi, rup)[lpos] = rhi[S * S3::kPS + lpos];
+    }
+  };
+  float2 p[SMAX][4], q[SMAX][4], dlo[SMAX][2];
+#pragma unroll
+  for (int sl = 0; sl < SMAX; ++sl) {
+    if (own && sl < S) {
+      float t[8];
+      ld8(rr32, grid3(P, ix, iy, lo + sl), t);
+      rlo[(sl + 1) * S3::kPS + lpos] = make_float4(t[0], t[1], t[2], t[3]);
+      rhi[(sl + 1) * S3::kPS + lpos] = make_float4(t[4], t[5], t[6], t[7]);
+      dhi[sl * S3::kMaxCol + ccol] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) p[sl][k] = q[sl][k] = f2(0.f, 0.f);
+    dlo[sl][0] = dlo[sl][1] = f2(0.f, 0.f);
+  }
+  if (tid < 8) cs.seg_beta[tid] = 0.0f;  // 0: p = r, q = A r on the first pass
+  push_halos();
+  csync<CS>();
+
+  int par = 0;
+  for (int iit = 0; iit < inner_maxit && iact; ++iit) {
+    // q = A~ r + beta q, p = r + beta p on the owned column; p.q
+#pragma unroll
+    for (int sl = 0; sl < SMAX; ++sl)
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        q[sl][k] = __fmul2_rn(f2(cs.seg_beta[2 * k], cs.seg_beta[2 * k + 1]), q[sl][k]);
+    if (own) {
+      slab_row<SMAX, -1>(rlo, rhi, cpl, lpos, ccol, S, q);
+      slab_row<SMAX, 0>(rlo, rhi, cpl, lpos, ccol, S, q);
+      slab_row<SMAX, 1>(rlo, rhi, cpl, lpos, ccol, S, q);
+    }
+    float2 sg2[4] = {f2(0.f, 0.f), f2(0.f, 0.f), f2(0.f, 0.f), f2(0.f, 0.f)};
+#pragma unroll
+    for (int sl = 0; sl < SMAX; ++sl) {
+      if (own && sl < S) {
+        const float4 a = rlo[(sl + 1) * S3::kPS + lpos], b = rhi[(sl + 1) * S3::kPS + lpos];
+        const float2 rv[4] = {f2(a.x, a.y), f2(a.z, a.w), f2(b.x, b.y), f2(b.z, b.w)};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          p[sl][k] = __ffma2_rn(f2(cs.seg_beta[2 * k], cs.seg_beta[2 * k + 1]), p[sl][k], rv[k]);
+          sg2[k] = __ffma2_rn(p[sl][k], q[sl][k], sg2[k]);
+        }
+      }
+    }
+    float sg[8] = {sg2[0].x, sg2[0].y, sg2[1].x, sg2[1].y, sg2[2].x, sg2[2].y, sg2[3].x, sg2[3].y};
+    cluster_sum8<NT, CS>(sg, redw, part, 0, lane, warp);
+    float al[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) al[k] = (((iact >> k) & 1u) && sg[k] > 0.f) ? cs.seg_rho[par][k] / sg[k] : 0.0f;
+    // d += alpha p, r -= alpha q (r in shared memory, pushed to the halos), r.r
+    float2 rp2[4] = {f2(0.f, 0.f), f2(0.f, 0.f), f2(0.f, 0.f), f2(0.f, 0.f)};
+#pragma unroll
+    for (int sl = 0; sl < SMAX; ++sl) {
+      if (own && sl < S) {
+        const int pi = (sl + 1) * S3::kPS + lpos;
+        const float4 a = rlo[pi], b = rhi[pi];
+        float2 rv[4] = {f2(a.x, a.y), f2(a.z, a.w), f2(b.x, b.y), f2(b.z, b.w)};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          rv[k] = __ffma2_rn(f2(-al[2 * k], -al[2 * k + 1]), q[sl][k], rv[k]);
+          rp2[k] = __ffma2_rn(rv[k], rv[k], rp2[k]);
+        }
+        rlo[pi] = make_float4(rv[0].x, rv[0].y, rv[1].x, rv[1].y);
+        rhi[pi] = make_float4(rv[2].x, rv[2].y, rv[3].x, rv[3].y);
+        dlo[sl][0] = __ffma2_rn(f2(al[0], al[1]), p[sl][0], dlo[sl][0]);
+        dlo[sl][1] = __ffma2_rn(f2(al[2], al[3]), p[sl][1], dlo[sl][1]);
+        float4 dh = dhi[sl * S3::kMaxCol + ccol];
+        const float2 d45 = __ffma2_rn(f2(al[4], al[5]), p[sl][2], f2(dh.x, dh.y));
+        const float2 d67 = __ffma2_rn(f2(al[6], al[7]), p[sl][3], f2(dh.z, dh.w));
+        dhi[sl * S3::kMaxCol + ccol] = make_float4(d45.x, d45.y, d67.x, d67.y);
+      }
+    }
+    push_halos();
+    float rp[8] = {rp2[0].x, rp2[0].y, rp2[1].x, rp2[1].y, rp2[2].x, rp2[2].y, rp2[3].x, rp2[3].y};
+    cluster_sum8<NT, CS>(rp, redw, part, 1, lane, warp);
+    if (tid < 8 && ((iact >> tid) & 1u)) cs.inner_iters[tid] += 1;
+    // beta and the next r.r by thread k; every thread updates the active set.
+    // The barrier below orders these writes before the next iteration's reads
+    // (and the reads of seg_rho[par] above before the next writes to it).
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      float be = 0.0f;
+      const float rho = cs.seg_rho[par][k];
+      float next = rho;
+      if ((iact >> k) & 1u) {
+        if (!(rp[k] <= cs.seg_thr[k]) && isfinite(rp[k])) {
+          be = rp[k] / rho;
+          next = rp[k];
+        } else {
+          iact &= ~(1u << k);
+        }
+      }
+      if (tid == k) {
+        cs.seg_rho[par ^ 1][k] = next;
+        cs.seg_beta[k] = be;
+      }
+    }
+    par ^= 1;
+    __syncthreads();
+  }
+  // the correction of the owned nodes, for the FP64 update of the whole cluster
+#pragma unroll
+  for (int sl = 0; sl < SMAX; ++sl)
+    if (own && sl < S) {
+      const float4 dh = dhi[sl * S3::kMaxCol + ccol];
+      const float dv[8] = {dlo[sl][0].x, dlo[sl][0].y, dlo[sl][1].x, dlo[sl][1].y, dh.x, dh.y, dh.z, dh.w};
+      st8(dd32, grid3(P, ix, iy, lo + sl), dv);
+    }
+  csync<CS>();
+}
+
 template <int NT, bool MIXED, int MINB, int CS>
 __global__ void __launch_bounds__(NT, MINB)
 msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t slot_bytes) {
@@ -610,7 +914,12 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
   constexpr int CNT = NT * CS;  // threads working on one cell (the cluster's)
   __shared__ CellShared3D cs;
   __shared__ double red[2][NW * 16];
-  __shared__ double redE[NW * 32];
+  // the slab cluster shape reuses its dynamic shared memory (idle in the
+  // epilogue) for the epilogue partials
+  constexpr bool kSlab = MIXED && CS > 1;
+  __shared__ double redE_static[kSlab ? 1 : NW * 32];
+  extern __shared__ __align__(16) unsigned char dsm3[];
+  double *redE = kSlab ? reinterpret_cast<double *>(dsm3) : redE_static;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int crank = cluster_rank<CS>();  // this CTA's rank in its cluster
   const int ctid = crank * NT + tid;     // thread index within the cluster
@@ -1153,14 +1462,19 @@ msfem3d_kernel(const KernelParams p, unsigned char *__restrict__ work, size_t sl
         __syncthreads();
         // N = 8, 16, 24 (the uneven 3D sphere workload) get the z-pair stencil
         // with compile-time offsets
-        if (N == 24)
+        if constexpr (CS > 1) {
+          // cluster shape: the slabs of the cell stay in the CTAs' shared memory
+          inner_segment3d_slab<NT, CS, (kNMax3D - 1 + CS - 1) / CS>(c32, rr32, dd32, G, N, P, p.inner_maxit, iact,
+                                                                   reinterpret_cast<float *>(red[0]), cs, dsm3);
+        } else if (N == 24) {
           inner_segment3d<NT, CS, 27>(c32, pp32, qq32, rr32, dd32, G, m, P, nI, p.inner_maxit, iact, buf, red, cs);
-        else if (N == 16)
+        } else if (N == 16) {
           inner_segment3d<NT, CS, 19>(c32, pp32, qq32, rr32, dd32, G, m, P, nI, p.inner_maxit, iact, buf, red, cs);
-        else if (N == 8)
+        } else if (N == 8) {
           inner_segment3d<NT, CS, 11>(c32, pp32, qq32, rr32, dd32, G, m, P, nI, p.inner_maxit, iact, buf, red, cs);
-        else
+        } else {
           inner_segment3d<NT, CS, 0>(c32, pp32, qq32, rr32, dd32, G, m, P, nI, p.inner_maxit, iact, buf, red, cs);
+        }
         // x~ += d (FP64); r = -(A~ phi~)_I in FP64
         for (int k = ctid; k < nI; k += CNT) {
           const int g = interior(k);

@@ -15,10 +15,12 @@
 
 #include <cmath>
 #include <map>
+#include <memory>
 #include <stdexcept>
 #include <vector>
 
 #include "diffusion_problem_basis.hpp"
+#include "global_q1.hpp"
 
 namespace DiffusionProblem {
 
@@ -78,116 +80,20 @@ class DiffusionProblemMultiscale {
     return ijk[0] + n * (ijk[1] + (dim == 3 ? n * ijk[2] : 0));
   }
 
+  // diffusion_problem_ms.tpp:159-255: element matrices and loads from the
+  // basis objects (the first getter flushes the GPU batch), Neumann terms,
+  // scatter into the global system
   void assemble_system() {
-    const unsigned int K = n_cells_per_dir();
-    size_t nn = 1;
-    for (int a = 0; a < dim; ++a) nn *= (K + 1);
-    A.assign(nn * nn, 0.0);
-    rhs.assign(nn, 0.0);
-    const double g[2] = {0.5 - 0.5 / std::sqrt(3.0), 0.5 + 0.5 / std::sqrt(3.0)};
-    Coefficients::NeumannBC<dim> neumann;
-    constexpr unsigned int nv = GeometryInfo<dim>::vertices_per_cell;
+    sys_ = std::make_unique<GlobalQ1System<dim>>(n_cells_per_dir(), bc);
     for (const auto &cell : cells_) {
       const auto &basis = cell_basis_map.at(cell.id());
-      const FullMatrix &M = basis.get_global_element_matrix();  // flushes the GPU batch
-      Vector F = basis.get_global_element_rhs();
-      const unsigned int c = cell.id().index();
-      const unsigned int ci[3] = {c % K, (c / K) % K, dim == 3 ? c / (K * K) : 0u};
-      if (bc == 0) {
-        // Neumann faces with odd boundary id, QGauss<dim-1>(2) (diffusion_problem_ms.tpp:206-235)
-        for (int a = 0; a < dim; ++a) {
-          if (ci[a] != K - 1) continue;
-          const int nfq = 1 << (dim - 1);
-          for (int fq = 0; fq < nfq; ++fq) {
-            double xi[3];
-            int bt = 0;
-            for (int e = 0; e < dim; ++e) {
-              if (e == a) { xi[e] = 1.0; continue; }
-              xi[e] = g[(fq >> bt) & 1];
-              ++bt;
-            }
-            Point<dim> x;
-            for (int e = 0; e < dim; ++e) x(e) = (ci[e] + xi[e]) / K;
-            const double gv = neumann.value(x);
-            const double JxW = std::pow(1.0 / K, dim - 1) / nfq;
-            for (unsigned int i = 0; i < nv; ++i) {
-              double psi = 1.0;
-              for (int e = 0; e < dim; ++e) psi *= ((i >> e) & 1) ? xi[e] : 1.0 - xi[e];
-              F(i) += gv * psi * JxW;
-            }
-          }
-        }
-      }
-      for (unsigned int i = 0; i < nv; ++i) {
-        unsigned int ni[3] = {0, 0, 0};
-        for (int a = 0; a < dim; ++a) ni[a] = ci[a] + ((i >> a) & 1);
-        const size_t gi = node_index(ni);
-        for (unsigned int j = 0; j < nv; ++j) {
-          unsigned int nj[3] = {0, 0, 0};
-          for (int a = 0; a < dim; ++a) nj[a] = ci[a] + ((j >> a) & 1);
-          A[gi * nn + node_index(nj)] += M(i, j);
-        }
-        rhs[gi] += F(i);
-      }
+      sys_->add_cell(cell.id().index(), basis.get_global_element_matrix(), basis.get_global_element_rhs());
     }
   }
 
-  void solve() {
-    const unsigned int K = n_cells_per_dir();
-    const size_t nn = rhs.size(), n = K + 1;
-    Coefficients::DirichletBC<dim> dirichlet;
-    std::vector<double> ud(nn, 0.0);
-    std::vector<char> fixed(nn, 0);
-    for (size_t g = 0; g < nn; ++g) {
-      const unsigned int ijk[3] = {unsigned(g % n), unsigned((g / n) % n), dim == 3 ? unsigned(g / (n * n)) : 0u};
-      bool lower = false, any = false;
-      Point<dim> x;
-      for (int a = 0; a < dim; ++a) {
-        x(a) = double(ijk[a]) / K;
-        if (ijk[a] == 0) lower = any = true;
-        if (ijk[a] == K) any = true;
-      }
-      if (bc == 0 && lower) { fixed[g] = 1; ud[g] = dirichlet.value(x); }
-      if (bc == 1 && any) { fixed[g] = 1; ud[g] = 0.0; }
-    }
-    std::vector<size_t> freeidx;
-    for (size_t g = 0; g < nn; ++g)
-      if (!fixed[g]) freeidx.push_back(g);
-    const size_t nf = freeidx.size();
-    std::vector<double> L(nf * nf), b(nf);
-    for (size_t r = 0; r < nf; ++r) {
-      double s = rhs[freeidx[r]];
-      for (size_t g = 0; g < nn; ++g)
-        if (fixed[g]) s -= A[freeidx[r] * nn + g] * ud[g];
-      b[r] = s;
-      for (size_t c = 0; c < nf; ++c) L[r * nf + c] = A[freeidx[r] * nn + freeidx[c]];
-    }
-    // dense Cholesky (coarse systems here are small)
-    for (size_t j = 0; j < nf; ++j) {
-      double s = L[j * nf + j];
-      for (size_t k = 0; k < j; ++k) s -= L[j * nf + k] * L[j * nf + k];
-      if (!(s > 0)) throw std::runtime_error("coarse matrix not positive definite");
-      const double d = std::sqrt(s);
-      L[j * nf + j] = d;
-      for (size_t i = j + 1; i < nf; ++i) {
-        double t = L[i * nf + j];
-        for (size_t k = 0; k < j; ++k) t -= L[i * nf + k] * L[j * nf + k];
-        L[i * nf + j] = t / d;
-      }
-    }
-    for (size_t i = 0; i < nf; ++i) {
-      double s = b[i];
-      for (size_t k = 0; k < i; ++k) s -= L[i * nf + k] * b[k];
-      b[i] = s / L[i * nf + i];
-    }
-    for (size_t i = nf; i-- > 0;) {
-      double s = b[i];
-      for (size_t k = i + 1; k < nf; ++k) s -= L[k * nf + i] * b[k];
-      b[i] = s / L[i * nf + i];
-    }
-    u = ud;
-    for (size_t r = 0; r < nf; ++r) u[freeidx[r]] = b[r];
-  }
+  // diffusion_problem_ms.tpp:258-296 (the reference's Trilinos solve): the
+  // Dirichlet data and a direct solve
+  void solve() { u = sys_->solve(); }
 
   void send_global_weights_to_cell() {
     const unsigned int K = n_cells_per_dir();
@@ -210,7 +116,8 @@ class DiffusionProblemMultiscale {
   std::vector<CoarseCell<dim>> cells_;
   std::map<CellId, DiffusionProblemBasis<dim>> cell_basis_map;
   bool output_first_ = false;
-  std::vector<double> A, rhs, u;
+  std::unique_ptr<GlobalQ1System<dim>> sys_;
+  std::vector<double> u;
 };
 
 }  // namespace DiffusionProblem

@@ -9,6 +9,7 @@
 #include <memory>
 #include <string>
 
+#include "diffusion_problem.hpp"
 #include "diffusion_problem_ms.hpp"
 
 namespace {
@@ -27,10 +28,10 @@ class LinearRhs : public Coefficients::ScalarFunction<dim> {
 
 enum { kOptRelativeTol = 1, kOptLinearRhs = 2, kOptOutputBasis = 4 };
 
+// Problem data of every flush: device, precision, coefficient, right-hand
+// side and stopping rule.
 template <int dim>
-int run_ms(int n_refine, int n_refine_local, int coef, const double *params, double f_value, int bc,
-           int precision, int device, double *u_out, double *M_out, double *F_out, double *fine_out,
-           int write_vtu, int options) {
+void configure(int coef, const double *params, double f_value, int precision, int device, int options) {
   using namespace DiffusionProblem;
   auto &batch = BasisBatch<dim>::get();
   batch.set_device(device);
@@ -52,6 +53,14 @@ int run_ms(int n_refine, int n_refine_local, int coef, const double *params, dou
       for (int j = i; j < dim; ++j, ++k) A[i][j] = A[j][i] = params[k];
     batch.set_coefficient(std::make_shared<Coefficients::ConstantCoeff<dim>>(A));
   }
+}
+
+template <int dim>
+int run_ms(int n_refine, int n_refine_local, int coef, const double *params, double f_value, int bc,
+           int precision, int device, double *u_out, double *M_out, double *F_out, double *fine_out,
+           int write_vtu, int options) {
+  using namespace DiffusionProblem;
+  configure<dim>(coef, params, f_value, precision, device, options);
   DiffusionProblemMultiscale<dim> ms(n_refine, n_refine_local, bc);
   ms.set_output_flag_first_cell(options & kOptOutputBasis);
   ms.run();
@@ -75,6 +84,18 @@ int run_ms(int n_refine, int n_refine_local, int coef, const double *params, dou
     if (write_vtu && c == 0) b.output_global_solution_in_cell();  // into the working directory
     ++c;
   }
+  return 0;
+}
+
+template <int dim>
+int run_fem(int n_refine, int coef, const double *params, double f_value, int bc, int precision, int device,
+            double *u_out, int write_vtu, int options) {
+  configure<dim>(coef, params, f_value, precision, device, options);
+  DiffusionProblem::DiffusionProblem<dim> fem(n_refine, bc);
+  fem.run();
+  const auto &u = fem.solution();
+  if (u_out) std::memcpy(u_out, u.data(), sizeof(double) * u.size());
+  if (write_vtu) fem.output_results();  // into the working directory
   return 0;
 }
 
@@ -106,6 +127,25 @@ int msfem_host_ms_run(int dim, int n_refine, int n_refine_local, int coef, const
     if (dim == 3)
       return run_ms<3>(n_refine, n_refine_local, coef, params, f_value, bc, precision, device, u_out,
                        M_out, F_out, fine_out, write_vtu, options);
+    g_err = "dim must be 2 or 3";
+    return -1;
+  } catch (const std::exception &e) {
+    g_err = e.what();
+    return -2;
+  }
+}
+
+// The standard Q1 FEM on the unit square/cube with 2^n_refine cells per
+// direction (DiffusionProblem<dim>::run, diffusion_problem.tpp:336-377): the
+// comparator the reference runs beside the MsFEM.  coef, params, f_value, bc,
+// precision, device and options as for msfem_host_ms_run; u [(K+1)^d]
+// lexicographic nodal solution; write_vtu: solution-std_<d>d_refinements-<n>
+// .0000.vtu in the working directory.
+int msfem_host_fem_run(int dim, int n_refine, int coef, const double *params, double f_value, int bc,
+                       int precision, int device, double *u_out, int write_vtu, int options) {
+  try {
+    if (dim == 2) return run_fem<2>(n_refine, coef, params, f_value, bc, precision, device, u_out, write_vtu, options);
+    if (dim == 3) return run_fem<3>(n_refine, coef, params, f_value, bc, precision, device, u_out, write_vtu, options);
     g_err = "dim must be 2 or 3";
     return -1;
   } catch (const std::exception &e) {

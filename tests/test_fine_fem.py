@@ -13,6 +13,8 @@ diffusion_problem.tpp) is the standard FEM solve.  Checked: the MsFEM's fine
 solution (msfem_reconstruct) is within 1% (relative l2 over the fine
 nodes; measured 0.53%) of the fine FEM, and over 10x closer than Q1 FEM on
 the coarse mesh (14.5%)."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -88,3 +90,47 @@ def test_gpu_msfem_against_fine_fem(pkg, oracle, engine):
     assert np.abs(fine["M"] - ref["M"]).max() < 1e-12 * np.abs(ref["M"]).max()
     assert e_ms < 0.01, e_ms
     assert e_ms < 0.1 * e_q1, (e_ms, e_q1)
+
+
+def fem_lib(pkg):
+    from test_host_mirror import host_lib
+
+    lib = host_lib(pkg)
+    vp = ctypes.c_void_p
+    lib.msfem_host_fem_run.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, ctypes.c_double,
+                                       ctypes.c_int, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, ctypes.c_int]
+    lib.msfem_host_fem_run.restype = ctypes.c_int
+    return lib
+
+
+def test_standard_fem_component_is_exported(built):
+    lib = fem_lib(built)
+    assert hasattr(lib, "msfem_host_fem_run")
+
+
+@pytest.mark.gpu
+def test_host_standard_fem_component(pkg, oracle, tmp_path, monkeypatch):
+    """DiffusionProblem<2> of the host library (the standard Q1 FEM the
+    reference runs beside the MsFEM, diffusion_problem.tpp:336-377) on the
+    128 x 128 fine mesh: its solution equals the oracle's fine FEM, it writes
+    solution-std_2d_refinements-7.0000.vtu, and the host MsFEM's fine solution
+    is within 1% of it."""
+    from test_host_mirror import run_host
+
+    monkeypatch.chdir(tmp_path)
+    lib = fem_lib(pkg)
+    W = pkg.workloads
+    u = np.zeros((KF + 1) ** 2)
+    params = np.zeros(8)
+    rc = lib.msfem_host_fem_run(2, 3 + L, 0, ctypes.c_void_p(params.ctypes.data), 2.0, 0, 0, 0,
+                                ctypes.c_void_p(u.ctypes.data), 1, 0)
+    assert rc == 0
+    fine = oracle.run(W.reference_problem(2, 3 + L, 0))
+    U_f = oracle.coarse_solve(2, KF, fine["M"], fine["F"], 0)
+    assert np.abs(u - U_f).max() < 1e-10 * np.abs(U_f).max()
+    assert (tmp_path / f"solution-std_2d_refinements-{3 + L}.0000.vtu").exists()
+    rc, msg, _, _, _, fine_ms = run_host(lib, 2, 3, L)
+    assert rc == 0, msg
+    U_ms = fine_grid(fine_ms)
+    e_ms = np.linalg.norm(U_ms - u.reshape(KF + 1, KF + 1)) / np.linalg.norm(u)
+    assert e_ms < 0.01, e_ms
