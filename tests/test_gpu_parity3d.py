@@ -105,3 +105,29 @@ def test_every_compiled_launch_shape_gives_the_same_answer_3d(pkg, oracle, engin
         assert np.abs(got["basis"] - ref["basis"]).max() < 1e-9, v
     engine.set_tuning({"dim": 3, "n_max": 9, "precision": prec, "variant": 0, "check_interval": 0,
                        "inner_tol": 1e-6})
+
+
+def test_slab_cluster_ragged_and_empty_slabs(pkg, oracle, engine):
+    """The mixed form's 8-CTA slab cluster on cells with fewer interior
+    planes than CTAs (N = 1, 2, 3, 5: empty slabs, no interior at N = 1)
+    next to the largest cell (N = 24) in one launch, against the oracle."""
+    W = pkg.workloads
+    rng = np.random.default_rng(12)
+    sp = np.column_stack([rng.uniform(0, 1, (300, 3)), rng.uniform(0.02, 0.05, 300)])
+    corners = W.unit_cube_corners(3, 4)[[3, 17, 30, 44, 60]]
+    nf = np.array([1, 2, 3, 5, 24], dtype=np.int32)
+    prob = W.problem(3, corners, nf, {"kind": 4, "params": [1e4], "spheres": sp})
+    probe = engine.autotune(prob, precision="mixed", tol=1e-12, sample_cells=5)
+    slab = probe["n_variants"] - 1  # the slab cluster is the last compiled mixed shape
+    engine.set_tuning({"dim": 3, "n_max": 24, "precision": 1, "variant": slab, "check_interval": 0,
+                       "inner_tol": 1e-6})
+    try:
+        got = engine.run(prob, precision="mixed", tol=1e-12, want_basis=True)
+    finally:
+        engine.set_tuning({"dim": 3, "n_max": 24, "precision": 1, "variant": 0, "check_interval": 0,
+                           "inner_tol": 1e-6})
+    ref = oracle.run(prob, want_basis=True)
+    assert got["rc"] == 0 and np.all(got["status"] == 0)
+    assert rel_err(got["M"], ref["M"]) < TOL_REL
+    assert rel_err(got["F"], ref["F"]) < TOL_REL
+    assert np.abs(got["basis"] - ref["basis"]).max() < 1e-9
