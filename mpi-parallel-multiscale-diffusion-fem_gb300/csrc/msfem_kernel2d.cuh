@@ -92,6 +92,34 @@ __device__ __forceinline__ void stencil9(const T *__restrict__ c, const T *__res
 #undef MSFEM_ACC
 }
 
+// y = A v at node g with the unscaled operator: diagonal d[g] and the 8
+// couplings of c (as stencil9), 4 RHS.
+__device__ __forceinline__ void stencil9_unscaled(const double *__restrict__ c, const double *__restrict__ d,
+                                                  const double *__restrict__ v, int g, int P, double (&y)[4]) {
+  double cc[4], t[4];
+  ld4(c, g, cc);
+  const double cW = c[4 * (g - 1) + 0];
+  const double cS = c[4 * (g - P) + 2];
+  const double cSW = c[4 * (g - P - 1) + 1];
+  const double cSE = c[4 * (g - P + 1) + 3];
+  const double dg = d[g];
+  ld4(v, g, y);
+#pragma unroll
+  for (int r = 0; r < 4; ++r) y[r] *= dg;
+#define MSFEM_ACC(OFF, COEF)                      \
+  ld4(v, g + (OFF), t);                           \
+  _Pragma("unroll") for (int r = 0; r < 4; ++r) y[r] = fma(COEF, t[r], y[r]);
+  MSFEM_ACC(1, cc[0])
+  MSFEM_ACC(-1, cW)
+  MSFEM_ACC(P, cc[2])
+  MSFEM_ACC(-P, cS)
+  MSFEM_ACC(P + 1, cc[1])
+  MSFEM_ACC(-P - 1, cSW)
+  MSFEM_ACC(P - 1, cc[3])
+  MSFEM_ACC(-P + 1, cSE)
+#undef MSFEM_ACC
+}
+
 // Block-uniform scalars of one cell, in shared memory.
 struct CellShared2D {
   double corners[8];
@@ -142,6 +170,60 @@ __device__ __forceinline__ void boundary_node(int k, int N, int &ix, int &iy) {
   else { ix = 0; iy = N - (k - 3 * N); }
 }
 
+// BasisQ1 data of a 2D cell (the q1_setup<2> interpolant) in closed form.
+// In the translated, scaled coordinates x' = (x - v0) / H vertex 0 sits at
+// the origin, so the Vandermonde row of vertex 0 is (1, 0, 0, 0): the
+// constant coefficient of basis i is delta_i0, and the other three solve
+// Q c = (delta_iv - delta_i0)_{v=1..3} with Q's rows (a_v, b_v, a_v b_v),
+// (a_v, b_v) = x'_v.  Q^-1 = adj(Q) / det(Q).  A single thread runs this
+// (about 70 FP64 operations instead of a pivoted elimination on a 4 x 8
+// array).  Returns false for a degenerate cell.
+__device__ inline bool q1_setup2d_closed(const double *cr, double *coef, double *shift, double *inv_scale) {
+  shift[0] = cr[0];
+  shift[1] = cr[1];
+  double H = 0.0;
+#pragma unroll
+  for (int v = 1; v < 4; ++v) H = fmax(H, fmax(fabs(cr[2 * v] - cr[0]), fabs(cr[2 * v + 1] - cr[1])));
+  if (!(H > 0.0)) return false;
+  const double ih = 1.0 / H;
+  *inv_scale = ih;
+  double a[3], b[3], e[3];
+#pragma unroll
+  for (int v = 0; v < 3; ++v) {
+    a[v] = (cr[2 * (v + 1)] - cr[0]) * ih;
+    b[v] = (cr[2 * (v + 1) + 1] - cr[1]) * ih;
+    e[v] = a[v] * b[v];
+  }
+  // cofactors C[v][m] of Q (v: vertex row 1..3, m: monomial x', y', x'y')
+  double C[3][3];
+  C[0][0] = b[1] * e[2] - e[1] * b[2];
+  C[0][1] = e[1] * a[2] - a[1] * e[2];
+  C[0][2] = a[1] * b[2] - b[1] * a[2];
+  C[1][0] = e[0] * b[2] - b[0] * e[2];
+  C[1][1] = a[0] * e[2] - e[0] * a[2];
+  C[1][2] = b[0] * a[2] - a[0] * b[2];
+  C[2][0] = b[0] * e[1] - e[0] * b[1];
+  C[2][1] = e[0] * a[1] - a[0] * e[1];
+  C[2][2] = a[0] * b[1] - b[0] * a[1];
+  const double det = a[0] * C[0][0] + b[0] * C[0][1] + e[0] * C[0][2];
+  if (!(fabs(det) > 0.0) || !isfinite(det)) return false;
+  const double idet = 1.0 / det;
+  coef[0] = 1.0;
+  coef[1] = coef[2] = coef[3] = 0.0;
+#pragma unroll
+  for (int m = 0; m < 3; ++m) {
+    double s = 0.0;
+#pragma unroll
+    for (int v = 0; v < 3; ++v) {
+      const double q = C[v][m] * idet;  // (Q^-1)[m][v]
+      coef[(m + 1) * 4 + v + 1] = q;
+      s += q;
+    }
+    coef[(m + 1) * 4] = -s;
+  }
+  return true;
+}
+
 // ---------------------------------------------------------------------------
 // Shared per-cell phases
 // ---------------------------------------------------------------------------
@@ -156,7 +238,7 @@ __device__ int cell_geometry2d(const KernelParams &p, CellShared2D &cs, int cell
     const double *cr = cs.corners;
     int st = MSFEM_CELL_CONVERGED;
     if (N < 1 || N > NMAX) st = MSFEM_CELL_BAD_INPUT;
-    if (st == MSFEM_CELL_CONVERGED && !q1_setup<2>(cr, cs.q1coef, cs.q1shift, &cs.q1iscale))
+    if (st == MSFEM_CELL_CONVERGED && !q1_setup2d_closed(cr, cs.q1coef, cs.q1shift, &cs.q1iscale))
       st = MSFEM_CELL_BAD_INPUT;
     // parallelogram test v0 + v3 == v1 + v2 (exact)
     const int aff = (cr[0] + cr[6] == cr[2] + cr[4]) && (cr[1] + cr[7] == cr[3] + cr[5]);
@@ -190,10 +272,15 @@ template <int NMAX, int NT>
 __device__ int cell_begin(const KernelParams &p, CellShared2D &cs, int cell, int N,
                           double *c64, double *v64, double *d64, float *v32, int tid) {
   const int P = N + 3, G = P * P;
-  for (int i = tid; i < 4 * G; i += NT) { c64[i] = 0.0; v64[i] = 0.0; }
-  for (int i = tid; i < G; i += NT) d64[i] = 0.0;
+  // 16-byte stores (every array starts on a 128-byte boundary)
+  const double2 z2 = make_double2(0.0, 0.0);
+  for (int i = tid; i < 2 * G; i += NT) {
+    reinterpret_cast<double2 *>(c64)[i] = z2;
+    reinterpret_cast<double2 *>(v64)[i] = z2;
+  }
+  for (int i = tid; i < (G + 1) / 2; i += NT) reinterpret_cast<double2 *>(d64)[i] = z2;
   if (v32)
-    for (int i = tid; i < 4 * G; i += NT) v32[i] = 0.0f;
+    for (int i = tid; i < G; i += NT) reinterpret_cast<float4 *>(v32)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
   if (tid < 4) { cs.iters[tid] = 0; cs.active[tid] = 1; cs.nu[tid] = 0.0; }
   return cell_geometry2d<NMAX>(p, cs, cell, N, tid);
 }
@@ -419,6 +506,51 @@ __device__ void scale2d(CellShared2D &cs, int N, double *c64, double *v64, const
   __syncthreads();
 }
 
+// Dirichlet data and FP32 scaling of the mixed form, which keeps its FP64
+// state unscaled: v64 holds phi = g_i on the boundary (BasisQ1 at the node)
+// and 0 inside, s32[4 g] the FP32 symmetric scaling d^-1/2 of interior node g
+// (0 on the boundary, so scaled couplings to boundary nodes vanish) for the
+// FP32 inner solve.  Non-positive or non-finite interior diagonals set
+// MSFEM_CELL_NAN.  s32 lives in the FP32 exchange buffer until the inner
+// solve overwrites it (every component other than [4 g] stays zero).
+template <int NT>
+__device__ void prepare2d_unscaled(CellShared2D &cs, int N, double *v64, const double *d64, float *s32,
+                                   int tid) {
+  const int P = N + 3, n = N + 1;
+  // boundary nodes in a loop of their own: FP64 work in divergent branches
+  // costs whole warp instructions, so the BasisQ1 evaluation runs converged
+  const double invN = 1.0 / (double)N;
+  for (int k = tid; k < 4 * N; k += NT) {
+    int bx, by;
+    boundary_node(k, N, bx, by);
+    const int g = (by + 1) * P + bx + 1;
+    double x[2], t[4];
+    bilinear_map(cs.corners, bx == N ? 1.0 : bx * invN, by == N ? 1.0 : by * invN, x);
+    q1_eval<2>(cs.q1coef, cs.q1shift, cs.q1iscale, x, t);
+    st4(v64, g, t);
+    s32[4 * g] = 0.0f;
+  }
+  // interior nodes (v64 is already zero there)
+  for (int k = tid; k < (N - 1) * (N - 1); k += NT) {
+    const int g = (k / (N - 1) + 2) * P + k % (N - 1) + 2;
+    const double d = d64[g];
+    if (!(d > 0.0) || !isfinite(d)) cs.status = MSFEM_CELL_NAN;
+    s32[4 * g] = rsqrtf((float)d);
+  }
+  __syncthreads();
+}
+
+// Interior node k of the ring next to the boundary (k < 4 (N - 2), N >= 3;
+// the single interior node for N = 2).
+__device__ __forceinline__ void ring_node(int k, int N, int &ix, int &iy) {
+  const int m = N - 2;
+  if (m <= 0) { ix = 1; iy = 1; }
+  else if (k < m) { ix = 1 + k; iy = 1; }
+  else if (k < 2 * m) { ix = N - 1; iy = 1 + (k - m); }
+  else if (k < 3 * m) { ix = N - 1 - (k - 2 * m); iy = N - 1; }
+  else { ix = 1; iy = N - 1 - (k - 3 * m); }
+}
+
 // Scaled boundary value phi~ at boundary node (ix, iy).
 __device__ __forceinline__ void boundary_value(const CellShared2D &cs, const double *d64, int N,
                                                int P, int ix, int iy, double (&t)[4]) {
@@ -481,13 +613,15 @@ __device__ inline double node_load(const KernelParams &p, const CellShared2D &cs
   return b;
 }
 
-// Epilogue contribution of node (ix, iy) with y = A~ phi~ known there.
+// Epilogue contribution of node (ix, iy) with y = A~ phi~ known there
+// (SCALED), or y = A phi with phi unscaled (the mixed form).
+template <bool SCALED = true>
 __device__ __forceinline__ void epilogue_node(const KernelParams &p, const CellShared2D &cs,
                                               const double *d64, int N, int P, int ix, int iy,
                                               const double (&ph)[4], const double (&y)[4],
                                               double (&acc)[32]) {
   const int g = (iy + 1) * P + ix + 1;
-  const double bl = node_load(p, cs, N, ix, iy) * rsqrt(d64[g]);
+  const double bl = SCALED ? node_load(p, cs, N, ix, iy) * rsqrt(d64[g]) : node_load(p, cs, N, ix, iy);
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
 #pragma unroll
@@ -542,8 +676,9 @@ __device__ void epilogue_finish(const KernelParams &p, CellShared2D &cs, int cel
   __syncthreads();
 }
 
-// Basis output phi = D^-1/2 phi~ (lexicographic nodes), when requested.
-template <int NT>
+// Basis output phi = D^-1/2 phi~ (lexicographic nodes), when requested;
+// SCALED = false: v64 holds phi itself.
+template <int NT, bool SCALED = true>
 __device__ void write_basis(const KernelParams &p, int cell, int N, const double *v64,
                             const double *d64, int tid) {
   if (!p.basis) return;
@@ -553,7 +688,7 @@ __device__ void write_basis(const KernelParams &p, int cell, int N, const double
     const int g = (k / n + 1) * P + k % n + 1;
     double ph[4];
     ld4(v64, g, ph);
-    const double s = rsqrt(d64[g]);
+    const double s = SCALED ? rsqrt(d64[g]) : 1.0;
 #pragma unroll
     for (int i = 0; i < 4; ++i) out[(int64_t)i * n * n + k] = ph[i] * s;
   }
@@ -982,6 +1117,7 @@ msfem2d_mixed_kernel(const KernelParams p) {
   constexpr int NW = NT / 32;
   static_assert((NMAX - 1) * ((NMAX - 1 + S - 1) / S) <= NT, "strips must cover the interior");
   static_assert(NW * 32 * sizeof(double) <= 16 * L::G, "epilogue partials fit in v32");
+  static_assert(4 * (NMAX - 2) <= NT, "the boundary-adjacent ring takes one node per thread");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double *c64 = reinterpret_cast<double *>(smem_raw + L::kC64);
   double *v64 = reinterpret_cast<double *>(smem_raw + L::kV64);
@@ -1019,7 +1155,10 @@ msfem2d_mixed_kernel(const KernelParams p) {
       __syncthreads();
       continue;
     }
-    scale2d<NT>(cs, N, c64, v64, d64, red[0], tid);
+    // The FP64 state stays unscaled (operator with its diagonal, phi = g on
+    // the boundary); only the FP32 inner solve works on the symmetrically
+    // scaled operator, with the scaling d^-1/2 computed in FP32.
+    prepare2d_unscaled<NT>(cs, N, v64, d64, v32, tid);
 
     // strip of this thread
     const int ncol = N - 1;
@@ -1030,29 +1169,41 @@ msfem2d_mixed_kernel(const KernelParams p) {
     const int ns = own ? min(S, N - s0) : 0;
     const int g0 = (s0 + 1) * P + ix + 1;
 
-    // FP64 right-hand sides b~ = -(A~ phi~)_I (and warm start).  phi~ is
-    // zero inside, so b~ vanishes at every node not next to the boundary:
-    // the stencil runs on the boundary-adjacent rows and columns only.
+    // FP64 right-hand sides b = -(A phi)_I (and warm start).  phi is zero
+    // inside, so b vanishes at every node not next to the boundary: one
+    // converged pass over that ring of 4 (N - 2) nodes computes it (one node
+    // per thread), and the strip owners pick it up from the interior entries
+    // of v64, which are zero until then.
     double r64[S][4];
     double bbp[4] = {0.0, 0.0, 0.0, 0.0};
-    const bool edge_col = ix == 1 || ix == N - 1;
+    const int nring = N >= 3 ? 4 * (N - 2) : (N == 2 ? 1 : 0);
+    double bk[4] = {0.0, 0.0, 0.0, 0.0};
+    int gk = -1;
+    if (tid < nring) {
+      int rx, ry;
+      ring_node(tid, N, rx, ry);
+      gk = (ry + 1) * P + rx + 1;
+      stencil9<double>(c64, v64, gk, P, bk);  // own value 0: no diagonal term
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        bk[r] = -bk[r];
+        bbp[r] = bk[r] * bk[r];
+      }
+    }
+    warp_partials<4>(bbp, red[1], warp, lane);
+    __syncthreads();  // every stencil read of v64 is done
+    if (gk >= 0) st4(v64, gk, bk);
+    __syncthreads();
 #pragma unroll
     for (int s = 0; s < S; ++s) {
 #pragma unroll
       for (int r = 0; r < 4; ++r) r64[s][r] = 0.0;
-      if (s < ns && (edge_col || s0 + s == 1 || s0 + s == N - 1)) {
-        double y[4];
-        stencil9<double>(c64, v64, g0 + s * P, P, y);
-        const double d = d64[g0 + s * P];
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-          r64[s][r] = -y[r];
-          bbp[r] = fma(r64[s][r] * d, r64[s][r], bbp[r]);
-        }
+      if (s < ns) {
+        ld4(v64, g0 + s * P, r64[s]);
+        const double z4[4] = {0.0, 0.0, 0.0, 0.0};
+        st4(v64, g0 + s * P, z4);  // the iterate starts at zero
       }
     }
-    warp_partials<4>(bbp, red[1], warp, lane);
-    __syncthreads();
     if (warp == 0) {
       const double t = warp_finish<4>(red[1], NW, lane);
       if (lane < 4) {
@@ -1068,10 +1219,9 @@ msfem2d_mixed_kernel(const KernelParams p) {
         if (s < ns) {
           const int g = g0 + s * P;
           const int node = (s0 + s) * n + ix;
-          const double sq = sqrt(d64[g]);
           double t[4];
 #pragma unroll
-          for (int r = 0; r < 4; ++r) t[r] = __ldg(wb + (int64_t)r * n * n + node) * sq;
+          for (int r = 0; r < 4; ++r) t[r] = __ldg(wb + (int64_t)r * n * n + node);
           st4(v64, g, t);
         }
       __syncthreads();
@@ -1079,26 +1229,31 @@ msfem2d_mixed_kernel(const KernelParams p) {
       for (int s = 0; s < S; ++s)
         if (s < ns) {
           double y[4];
-          stencil9<double>(c64, v64, g0 + s * P, P, y);
+          stencil9_unscaled(c64, d64, v64, g0 + s * P, P, y);
 #pragma unroll
           for (int r = 0; r < 4; ++r) r64[s][r] = -y[r];
         }
     }
-    // FP32 couplings of the strip: E, W, N, S, NE, SW, NW, SE of every row
+    // FP32 couplings of the strip, symmetrically scaled in FP32 (s = d^-1/2
+    // from v32[4 g], 0 on the boundary): E, W, N, S, NE, SW, NW, SE of every
+    // row; sown the strip's own scaling for the residual and the correction
     StripCoup<S> cp;
+    float sown[S];
     float gmax = 0.0f;  // Gershgorin bound of A~ (unit diagonal) over the strip
 #pragma unroll
     for (int s = 0; s < S; ++s) {
       const int g = g0 + s * P;
       const bool v = s < ns;
-      cp.cE[s] = v ? (float)c64[4 * g + 0] : 0.f;
-      cp.cNE[s] = v ? (float)c64[4 * g + 1] : 0.f;
-      cp.cN[s] = v ? (float)c64[4 * g + 2] : 0.f;
-      cp.cNW[s] = v ? (float)c64[4 * g + 3] : 0.f;
-      cp.cW[s] = v ? (float)c64[4 * (g - 1) + 0] : 0.f;
-      cp.cS[s] = v ? (float)c64[4 * (g - P) + 2] : 0.f;
-      cp.cSW[s] = v ? (float)c64[4 * (g - P - 1) + 1] : 0.f;
-      cp.cSE[s] = v ? (float)c64[4 * (g - P + 1) + 3] : 0.f;
+      const float sg = v ? v32[4 * g] : 0.f;
+      sown[s] = sg;
+      cp.cE[s] = v ? (float)c64[4 * g + 0] * sg * v32[4 * (g + 1)] : 0.f;
+      cp.cNE[s] = v ? (float)c64[4 * g + 1] * sg * v32[4 * (g + P + 1)] : 0.f;
+      cp.cN[s] = v ? (float)c64[4 * g + 2] * sg * v32[4 * (g + P)] : 0.f;
+      cp.cNW[s] = v ? (float)c64[4 * g + 3] * sg * v32[4 * (g + P - 1)] : 0.f;
+      cp.cW[s] = v ? (float)c64[4 * (g - 1) + 0] * sg * v32[4 * (g - 1)] : 0.f;
+      cp.cS[s] = v ? (float)c64[4 * (g - P) + 2] * sg * v32[4 * (g - P)] : 0.f;
+      cp.cSW[s] = v ? (float)c64[4 * (g - P - 1) + 1] * sg * v32[4 * (g - P - 1)] : 0.f;
+      cp.cSE[s] = v ? (float)c64[4 * (g - P + 1) + 3] * sg * v32[4 * (g - P + 1)] : 0.f;
       gmax = fmaxf(gmax, 1.0f + fabsf(cp.cE[s]) + fabsf(cp.cW[s]) + fabsf(cp.cN[s]) + fabsf(cp.cS[s]) +
                              fabsf(cp.cNE[s]) + fabsf(cp.cSW[s]) + fabsf(cp.cNW[s]) + fabsf(cp.cSE[s]));
     }
@@ -1151,9 +1306,8 @@ msfem2d_mixed_kernel(const KernelParams p) {
 #pragma unroll
       for (int s = 0; s < S; ++s)
         if (s < ns) {
-          const double d = d64[g0 + s * P];
 #pragma unroll
-          for (int r = 0; r < 4; ++r) nup[r] = fma(r64[s][r] * d, r64[s][r], nup[r]);
+          for (int r = 0; r < 4; ++r) nup[r] = fma(r64[s][r], r64[s][r], nup[r]);
         }
       warp_partials<4>(nup, red[0], warp, lane);
       __syncthreads();
@@ -1195,7 +1349,7 @@ msfem2d_mixed_kernel(const KernelParams p) {
         for (int s = 0; s < S; ++s) {
   #pragma unroll
           for (int r = 0; r < 4; ++r) {
-            rv[s][r] = s < ns ? (float)r64[s][r] * act[r] : 0.0f;
+            rv[s][r] = s < ns ? (float)r64[s][r] * sown[s] * act[r] : 0.0f;
             pv[s][r] = rv[s][r];
             dv[s][r] = 0.0f;
             qv[s][r] = 0.0f;
@@ -1335,7 +1489,7 @@ msfem2d_mixed_kernel(const KernelParams p) {
         for (int s = 0; s < S; ++s)
 #pragma unroll
           for (int r = 0; r < 4; ++r) {
-            rv[s][r] = s < ns ? (float)r64[s][r] * act[r] : 0.0f;
+            rv[s][r] = s < ns ? (float)r64[s][r] * sown[s] * act[r] : 0.0f;
             dv[s][r] = 0.0f;
           }
         auto apply_prec = [&]() {
@@ -1446,14 +1600,14 @@ msfem2d_mixed_kernel(const KernelParams p) {
         }
         __syncthreads();  // last reads of v32 / v32b before the next writes
       }
-      // ---- x~ += d (FP64), new FP64 residual r = -(A~ phi~)_I
+      // ---- x += s d (FP64), new FP64 residual r = -(A phi)_I
 #pragma unroll
       for (int s = 0; s < S; ++s)
         if (s < ns) {
           double xs[4];
           ld4(v64, g0 + s * P, xs);
 #pragma unroll
-          for (int r = 0; r < 4; ++r) xs[r] += (double)dv[s][r];
+          for (int r = 0; r < 4; ++r) xs[r] += (double)(dv[s][r] * sown[s]);
           st4(v64, g0 + s * P, xs);
         }
       __syncthreads();
@@ -1461,7 +1615,7 @@ msfem2d_mixed_kernel(const KernelParams p) {
       for (int s = 0; s < S; ++s)
         if (s < ns) {
           double y[4];
-          stencil9<double>(c64, v64, g0 + s * P, P, y);
+          stencil9_unscaled(c64, d64, v64, g0 + s * P, P, y);
 #pragma unroll
           for (int r = 0; r < 4; ++r) r64[s][r] = -y[r];
         }
@@ -1469,7 +1623,7 @@ msfem2d_mixed_kernel(const KernelParams p) {
     if (tid == 0) cs.refinements = ref;
 
     // ---------------- epilogue ----------------------------------------
-    // interior: A~ phi~ = -r (the converged FP64 residual, in registers)
+    // interior: A phi = -r (the converged FP64 residual, in registers)
     double acc[32];
 #pragma unroll
     for (int i = 0; i < 32; ++i) acc[i] = 0.0;
@@ -1480,7 +1634,7 @@ msfem2d_mixed_kernel(const KernelParams p) {
         ld4(v64, g0 + s * P, ph);
 #pragma unroll
         for (int r = 0; r < 4; ++r) y[r] = -r64[s][r];
-        epilogue_node(p, cs, d64, N, P, ix, s0 + s, ph, y, acc);
+        epilogue_node<false>(p, cs, d64, N, P, ix, s0 + s, ph, y, acc);
       }
     // boundary rows: stencil of the unconstrained matrix
     for (int k = tid; k < 4 * N; k += NT) {
@@ -1488,11 +1642,11 @@ msfem2d_mixed_kernel(const KernelParams p) {
       boundary_node(k, N, bx, by);
       const int g = (by + 1) * P + bx + 1;
       double y[4], ph[4];
-      stencil9<double>(c64, v64, g, P, y);
+      stencil9_unscaled(c64, d64, v64, g, P, y);
       ld4(v64, g, ph);
-      epilogue_node(p, cs, d64, N, P, bx, by, ph, y, acc);
+      epilogue_node<false>(p, cs, d64, N, P, bx, by, ph, y, acc);
     }
-    write_basis<NT>(p, cell, N, v64, d64, tid);
+    write_basis<NT, false>(p, cell, N, v64, d64, tid);
     __syncthreads();  // v32 is reused for the 32-value partials below
     epilogue_finish<NT, true>(p, cs, cell, acc, reinterpret_cast<double *>(v32), true, total_iters, tid);
   }
