@@ -67,6 +67,27 @@ __device__ __forceinline__ void st4(float *__restrict__ v, int g, const float (&
   *reinterpret_cast<float4 *>(v + 4 * g) = make_float4(t[0], t[1], t[2], t[3]);
 }
 
+// FP32 -> FP64 conversion by the IEEE-754 bit layouts, on the integer pipe
+// (measured cheaper than the conversion instruction in the mixed kernel's
+// FP64 update).  Exact for normal numbers and zeros; FP32 subnormals become
+// signed zeros, inf/NaN stay inf/NaN.
+__device__ __forceinline__ double f32_to_f64(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xFFu;
+  const uint32_t hi_sign = u & 0x80000000u;
+  const uint32_t m = u & 0x7FFFFFu;
+  uint32_t hi, lo;
+  if (e == 0u) {
+    hi = hi_sign;
+    lo = 0u;
+  } else {
+    const uint32_t ed = e == 0xFFu ? 0x7FFu : e + (1023u - 127u);
+    hi = hi_sign | (ed << 20) | (m >> 3);
+    lo = m << 29;
+  }
+  return __hiloint2double((int)hi, (int)lo);
+}
+
 // y = A~ v at node g (unit diagonal + 8 scaled couplings), 4 RHS.
 template <typename T>
 __device__ __forceinline__ void stencil9(const T *__restrict__ c, const T *__restrict__ v,
@@ -418,7 +439,11 @@ __device__ __forceinline__ bool element2d(const KernelParams &p, const CellShare
 }
 
 // Assembly: 4-colour scatter of the element matrices into the node stencil.
-template <int NT>
+// NODIAG: the element diagonals are not formed; every node's diagonal is
+// minus the sum of its 8 couplings afterwards (Q1 element matrices have zero
+// row sums: constants lie in the kernel of the gradient), which saves FP64
+// work per element at the price of 7 additions per node.
+template <int NT, bool NODIAG = false>
 __device__ void assemble2d(const KernelParams &p, CellShared2D &cs, int cell, int N,
                            double *c64, double *d64, int tid) {
   const int P = N + 3, nfc = N * N;
@@ -435,13 +460,25 @@ __device__ void assemble2d(const KernelParams &p, CellShared2D &cs, int cell, in
       if (!element2d(p, cs, tab, N, cx, cy, need_x, Kd, Ko)) cs.status = MSFEM_CELL_BAD_INPUT;
       const int g0 = (cy + 1) * P + cx + 1;
       const int g1 = g0 + 1, g2 = g0 + P, g3 = g0 + P + 1;
-      d64[g0] += Kd[0]; d64[g1] += Kd[1]; d64[g2] += Kd[2]; d64[g3] += Kd[3];
+      if (!NODIAG) { d64[g0] += Kd[0]; d64[g1] += Kd[1]; d64[g2] += Kd[2]; d64[g3] += Kd[3]; }
       c64[4 * g0 + 0] += Ko[0];  // E  of node 0 (0-1)
       c64[4 * g2 + 0] += Ko[5];  // E  of node 2 (2-3)
       c64[4 * g0 + 2] += Ko[1];  // N  of node 0 (0-2)
       c64[4 * g1 + 2] += Ko[4];  // N  of node 1 (1-3)
       c64[4 * g0 + 1] += Ko[2];  // NE of node 0 (0-3)
       c64[4 * g1 + 3] += Ko[3];  // NW of node 1 (1-2)
+    }
+    __syncthreads();
+  }
+  if constexpr (NODIAG) {
+    const int n = N + 1;
+    for (int k = tid; k < n * n; k += NT) {
+      const int g = (k / n + 1) * P + k % n + 1;
+      double cc[4];
+      ld4(c64, g, cc);
+      d64[g] = -(((cc[0] + cc[1]) + (cc[2] + cc[3])) +
+                 ((c64[4 * (g - 1) + 0] + c64[4 * (g - P) + 2]) +
+                  (c64[4 * (g - P - 1) + 1] + c64[4 * (g - P + 1) + 3])));
     }
     __syncthreads();
   }
@@ -628,6 +665,74 @@ __device__ __forceinline__ void epilogue_node(const KernelParams &p, const CellS
     for (int j = 0; j < 4; ++j) acc[4 * i + j] = fma(ph[i], y[j], acc[4 * i + j]);
     acc[16 + i] = fma(ph[i], bl, acc[16 + i]);
   }
+}
+
+// Symmetric epilogue of the mixed form: acc[16] holds M_ij for i <= j in the
+// order of sym_pair (10 values) and F (4); y = A phi at the node, phi unscaled.
+__device__ __forceinline__ void sym_pair(int v, int &i, int &j) {
+  // (0,0) (0,1) (0,2) (0,3) (1,1) (1,2) (1,3) (2,2) (2,3) (3,3)
+  i = v < 4 ? 0 : v < 7 ? 1 : v < 9 ? 2 : 3;
+  j = v < 4 ? v : v < 7 ? v - 3 : v < 9 ? v - 5 : 3;
+}
+__device__ __forceinline__ void epilogue_node_sym(const KernelParams &p, const CellShared2D &cs, int N,
+                                                  int ix, int iy, const double (&ph)[4], const double (&y)[4],
+                                                  double (&acc)[16]) {
+  const double bl = node_load(p, cs, N, ix, iy);
+#pragma unroll
+  for (int v = 0; v < 10; ++v) {
+    int i, j;
+    sym_pair(v, i, j);
+    acc[v] = fma(ph[i], y[j], acc[v]);
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) acc[10 + i] = fma(ph[i], bl, acc[10 + i]);
+}
+
+// Final block reduction of the symmetric epilogue (M mirrored) and the output
+// writes of the mixed form; the relative residual comes from cs.nu.
+template <int NT>
+__device__ void epilogue_finish_sym(const KernelParams &p, CellShared2D &cs, int cell, double (&acc)[16],
+                                    double *red16, const int (&total_iters)[4], int tid) {
+  constexpr int NW = NT / 32;
+  const int lane = tid & 31, warp = tid >> 5;
+  const double tot = warp_transpose_reduce<16>(acc, lane);
+  if ((lane & 1) == 0) red16[warp * 16 + (lane >> 1)] = tot;
+  __syncthreads();
+  if (warp == 0) {
+    double s = 0.0;
+    if (lane < 16)
+      for (int w = 0; w < NW; ++w) s += red16[w * 16 + lane];
+    if (lane < 10) {
+      int i, j;
+      sym_pair(lane, i, j);
+      p.M[(int64_t)cell * 16 + 4 * i + j] = s;
+      p.M[(int64_t)cell * 16 + 4 * j + i] = s;
+    } else if (lane < 14) {
+      p.F[(int64_t)cell * 4 + (lane - 10)] = s;
+    }
+    double rel = 0.0;
+    if (lane < 4) {
+      const double bb = cs.bb[lane];
+      const double nu = cs.nu[lane];
+      rel = bb > 0.0 ? sqrt(nu / bb) : sqrt(nu);
+    }
+#pragma unroll
+    for (int m = 2; m >= 1; m >>= 1) rel = fmax(rel, shfl_xor_d(rel, m));
+    if (lane < 4 && p.iters) p.iters[(int64_t)cell * 4 + lane] = total_iters[lane];
+    if (lane == 0) {
+      int st = cs.status;
+      for (int r = 0; r < 4; ++r) {
+        const int itv = cs.iters[r];
+        if (itv <= -1000000) st = st == MSFEM_CELL_CONVERGED ? MSFEM_CELL_MAXIT : st;
+        else if (itv < 0) st = MSFEM_CELL_NAN;
+      }
+      if (!isfinite(rel)) st = MSFEM_CELL_NAN;
+      p.status[cell] = st;
+      if (p.rel_res) p.rel_res[cell] = rel;
+      if (p.refinements) p.refinements[cell] = cs.refinements;
+    }
+  }
+  __syncthreads();
 }
 
 // Final block reduction of the 32 epilogue values and the output writes.
@@ -1149,7 +1254,7 @@ msfem2d_mixed_kernel(const KernelParams p) {
     }
     if constexpr (M > 0 && MINB < 2)
       for (int i = tid; i < 4 * (N + 3) * (N + 3); i += NT) v32b[i] = 0.0f;
-    assemble2d<NT>(p, cs, cell, N, c64, d64, tid);
+    assemble2d<NT, true>(p, cs, cell, N, c64, d64, tid);
     if (cs.status != MSFEM_CELL_CONVERGED) {
       cell_report_bad(p, cs, cell, tid);
       __syncthreads();
@@ -1246,14 +1351,14 @@ msfem2d_mixed_kernel(const KernelParams p) {
       const bool v = s < ns;
       const float sg = v ? v32[4 * g] : 0.f;
       sown[s] = sg;
-      cp.cE[s] = v ? (float)c64[4 * g + 0] * sg * v32[4 * (g + 1)] : 0.f;
-      cp.cNE[s] = v ? (float)c64[4 * g + 1] * sg * v32[4 * (g + P + 1)] : 0.f;
-      cp.cN[s] = v ? (float)c64[4 * g + 2] * sg * v32[4 * (g + P)] : 0.f;
-      cp.cNW[s] = v ? (float)c64[4 * g + 3] * sg * v32[4 * (g + P - 1)] : 0.f;
-      cp.cW[s] = v ? (float)c64[4 * (g - 1) + 0] * sg * v32[4 * (g - 1)] : 0.f;
-      cp.cS[s] = v ? (float)c64[4 * (g - P) + 2] * sg * v32[4 * (g - P)] : 0.f;
-      cp.cSW[s] = v ? (float)c64[4 * (g - P - 1) + 1] * sg * v32[4 * (g - P - 1)] : 0.f;
-      cp.cSE[s] = v ? (float)c64[4 * (g - P + 1) + 3] * sg * v32[4 * (g - P + 1)] : 0.f;
+      cp.cE[s] = v ? (float)(c64[4 * g + 0]) * sg * v32[4 * (g + 1)] : 0.f;
+      cp.cNE[s] = v ? (float)(c64[4 * g + 1]) * sg * v32[4 * (g + P + 1)] : 0.f;
+      cp.cN[s] = v ? (float)(c64[4 * g + 2]) * sg * v32[4 * (g + P)] : 0.f;
+      cp.cNW[s] = v ? (float)(c64[4 * g + 3]) * sg * v32[4 * (g + P - 1)] : 0.f;
+      cp.cW[s] = v ? (float)(c64[4 * (g - 1) + 0]) * sg * v32[4 * (g - 1)] : 0.f;
+      cp.cS[s] = v ? (float)(c64[4 * (g - P) + 2]) * sg * v32[4 * (g - P)] : 0.f;
+      cp.cSW[s] = v ? (float)(c64[4 * (g - P - 1) + 1]) * sg * v32[4 * (g - P - 1)] : 0.f;
+      cp.cSE[s] = v ? (float)(c64[4 * (g - P + 1) + 3]) * sg * v32[4 * (g - P + 1)] : 0.f;
       gmax = fmaxf(gmax, 1.0f + fabsf(cp.cE[s]) + fabsf(cp.cW[s]) + fabsf(cp.cN[s]) + fabsf(cp.cS[s]) +
                              fabsf(cp.cNE[s]) + fabsf(cp.cSW[s]) + fabsf(cp.cNW[s]) + fabsf(cp.cSE[s]));
     }
@@ -1607,7 +1712,7 @@ msfem2d_mixed_kernel(const KernelParams p) {
           double xs[4];
           ld4(v64, g0 + s * P, xs);
 #pragma unroll
-          for (int r = 0; r < 4; ++r) xs[r] += (double)(dv[s][r] * sown[s]);
+          for (int r = 0; r < 4; ++r) xs[r] += f32_to_f64(dv[s][r] * sown[s]);
           st4(v64, g0 + s * P, xs);
         }
       __syncthreads();
@@ -1623,10 +1728,11 @@ msfem2d_mixed_kernel(const KernelParams p) {
     if (tid == 0) cs.refinements = ref;
 
     // ---------------- epilogue ----------------------------------------
-    // interior: A phi = -r (the converged FP64 residual, in registers)
-    double acc[32];
+    // interior: A phi = -r (the converged FP64 residual, in registers); M is
+    // symmetric, so 10 of its entries are accumulated
+    double acc[16];
 #pragma unroll
-    for (int i = 0; i < 32; ++i) acc[i] = 0.0;
+    for (int i = 0; i < 16; ++i) acc[i] = 0.0;
 #pragma unroll
     for (int s = 0; s < S; ++s)
       if (s < ns) {
@@ -1634,7 +1740,7 @@ msfem2d_mixed_kernel(const KernelParams p) {
         ld4(v64, g0 + s * P, ph);
 #pragma unroll
         for (int r = 0; r < 4; ++r) y[r] = -r64[s][r];
-        epilogue_node<false>(p, cs, d64, N, P, ix, s0 + s, ph, y, acc);
+        epilogue_node_sym(p, cs, N, ix, s0 + s, ph, y, acc);
       }
     // boundary rows: stencil of the unconstrained matrix
     for (int k = tid; k < 4 * N; k += NT) {
@@ -1644,11 +1750,11 @@ msfem2d_mixed_kernel(const KernelParams p) {
       double y[4], ph[4];
       stencil9_unscaled(c64, d64, v64, g, P, y);
       ld4(v64, g, ph);
-      epilogue_node<false>(p, cs, d64, N, P, bx, by, ph, y, acc);
+      epilogue_node_sym(p, cs, N, bx, by, ph, y, acc);
     }
     write_basis<NT, false>(p, cell, N, v64, d64, tid);
     __syncthreads();  // v32 is reused for the 32-value partials below
-    epilogue_finish<NT, true>(p, cs, cell, acc, reinterpret_cast<double *>(v32), true, total_iters, tid);
+    epilogue_finish_sym<NT>(p, cs, cell, acc, reinterpret_cast<double *>(v32), total_iters, tid);
   }
 }
 

@@ -218,17 +218,18 @@ def test_every_compiled_launch_shape_gives_the_same_answer(pkg, oracle, engine, 
 @pytest.mark.parametrize("warm", [False, True])
 def test_every_mixed_shape_on_ragged_sizes(pkg, oracle, engine, warm):
     """Every compiled mixed launch shape of the N <= 32 class on cells with N
-    from 17 to 32 in one launch (partial thread strips, rows shorter than the
-    class), cold and warm-started from the oracle's basis plus a perturbation."""
+    from 1 to 32 in one launch (partial thread strips, rows shorter than the
+    class, cells without interior nodes), cold and warm-started from the
+    oracle's basis plus a perturbation."""
     W = pkg.workloads
-    nf = np.array([17, 18, 21, 24, 27, 29, 30, 31, 32], dtype=np.int32)
-    prob = W.problem(2, W.unit_cube_corners(2, 3), nf, {"kind": 1}, f_value=2.0)
+    nf = np.array([17, 18, 21, 24, 27, 29, 30, 31, 32, 1, 2, 3, 5, 8, 16, 32], dtype=np.int32)
+    prob = W.problem(2, W.unit_cube_corners(2, 4), nf, {"kind": 1}, f_value=2.0)
     ref = oracle.run(prob, want_basis=True)
     warm_basis = None
     if warm:
         rng = np.random.default_rng(11)
         warm_basis = ref["basis"] + 1e-3 * rng.standard_normal(ref["basis"].shape)
-    probe = engine.autotune(prob, precision="mixed", tol=1e-13, sample_cells=9)
+    probe = engine.autotune(prob, precision="mixed", tol=1e-13, sample_cells=16)
     assert probe["n_variants"] >= 1
     try:
         for v in range(probe["n_variants"]):
