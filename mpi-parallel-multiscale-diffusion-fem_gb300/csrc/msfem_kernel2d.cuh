@@ -1220,7 +1220,10 @@ __global__ void __launch_bounds__(NT, MINB)
 msfem2d_mixed_kernel(const KernelParams p) {
   using L = Smem2D<NMAX>;
   constexpr int NW = NT / 32;
-  static_assert((NMAX - 1) * ((NMAX - 1 + S - 1) / S) <= NT, "strips must cover the interior");
+  // threads per row-block of strips: the interior columns rounded up to a
+  // multiple of 8 lanes (one quarter-warp of 16-byte accesses)
+  constexpr int kSlots = (NMAX - 1 + 7) / 8 * 8;
+  static_assert(kSlots * ((NMAX - 1 + S - 1) / S) <= NT, "strips must cover the interior");
   static_assert(NW * 32 * sizeof(double) <= 16 * L::G, "epilogue partials fit in v32");
   static_assert(4 * (NMAX - 2) <= NT, "the boundary-adjacent ring takes one node per thread");
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1265,12 +1268,15 @@ msfem2d_mixed_kernel(const KernelParams p) {
     // scaled operator, with the scaling d^-1/2 computed in FP32.
     prepare2d_unscaled<NT>(cs, N, v64, d64, v32, tid);
 
-    // strip of this thread
+    // strip of this thread: SLOTS threads per row-block of strips (lane =
+    // column), so a quarter-warp never straddles two row-blocks and every
+    // 16-byte shared access of the strip loops is one contiguous wavefront
     const int ncol = N - 1;
     const int nstrip = ncol > 0 ? (ncol + S - 1) / S : 0;
-    const bool own = tid < ncol * nstrip;
-    const int ix = own ? 1 + tid % ncol : 1;
-    const int s0 = own ? 1 + S * (tid / ncol) : 1;
+    const int col = tid % kSlots, blk = tid / kSlots;
+    const bool own = col < ncol && blk < nstrip;
+    const int ix = own ? 1 + col : 1;
+    const int s0 = own ? 1 + S * blk : 1;
     const int ns = own ? min(S, N - s0) : 0;
     const int g0 = (s0 + 1) * P + ix + 1;
 

@@ -92,8 +92,9 @@ def test_tabulation_matches_oracle_3d(pkg, oracle, engine, ncomp):
     assert np.abs(a - b).max() < 1e-12 * np.abs(b).max()
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("geom", ["parallelogram", "bilinear"])
-def test_general_geometry(pkg, oracle, engine, geom):
+def test_general_geometry(pkg, oracle, engine, geom, precision):
     W = pkg.workloads
     c = W.unit_cube_corners(2, 4) * 0.8 + 0.05
     if geom == "parallelogram":
@@ -102,7 +103,7 @@ def test_general_geometry(pkg, oracle, engine, geom):
         rng = np.random.default_rng(7)
         c = c + rng.uniform(-0.01, 0.01, size=c.shape) * np.array([1, 1])
     prob = W.problem(2, c, 12, {"kind": 1}, f_value=2.0)
-    got = engine.run(prob, precision="fp64", tol=1e-13, want_basis=True)
+    got = engine.run(prob, precision=precision, tol=1e-13, want_basis=True)
     ref = oracle.run(prob, want_basis=True)
     check(got, ref)
 
@@ -240,6 +241,28 @@ def test_every_mixed_shape_on_ragged_sizes(pkg, oracle, engine, warm):
                 check(got, ref)
     finally:
         engine.set_tuning({"dim": 2, "n_max": 32, "precision": 1, "variant": 0, "check_interval": 0,
+                           "inner_tol": 1e-6})
+
+
+def test_every_mixed_shape_on_ragged_sizes_16(pkg, oracle, engine):
+    """The N <= 16 class: every compiled mixed shape on N = 1 ... 16 in one
+    launch, on bilinear cells (general geometry in the mixed form)."""
+    W = pkg.workloads
+    nf = np.array([1, 2, 3, 4, 5, 7, 9, 11, 12, 13, 14, 15, 16, 16, 8, 6], dtype=np.int32)
+    c = W.unit_cube_corners(2, 4) * 0.8 + 0.05
+    c = c + np.random.default_rng(9).uniform(-0.01, 0.01, size=c.shape)
+    prob = W.problem(2, c, nf, {"kind": 1}, f_value=2.0)
+    ref = oracle.run(prob, want_basis=True)
+    probe = engine.autotune(prob, precision="mixed", tol=1e-13, sample_cells=16)
+    try:
+        for v in range(probe["n_variants"]):
+            for ratio in (10.0, 100.0):
+                engine.set_tuning({"dim": 2, "n_max": 16, "precision": 1, "variant": v, "check_interval": 0,
+                                   "inner_tol": 1e-5, "cheb_ratio": ratio})
+                got = engine.run(prob, precision="mixed", tol=1e-13, want_basis=True)
+                check(got, ref)
+    finally:
+        engine.set_tuning({"dim": 2, "n_max": 16, "precision": 1, "variant": 0, "check_interval": 0,
                            "inner_tol": 1e-6})
 
 
