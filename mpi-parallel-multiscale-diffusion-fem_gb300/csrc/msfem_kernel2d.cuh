@@ -520,20 +520,25 @@ __device__ void scale2d(CellShared2D &cs, int N, double *c64, double *v64, const
   for (int m = 16; m >= 1; m >>= 1) dmin_part = fmin(dmin_part, shfl_xor_d(dmin_part, m));
   if (lane == 0) red[warp] = dmin_part;
   __syncthreads();
-  // Dirichlet data phi~_i = D^1/2 g_i (BasisQ1 at the node); interior 0
-  for (int k = tid; k < n * n; k += NT) {
-    const int ix = k % n, iy = k / n;
-    const int g = (iy + 1) * P + ix + 1;
-    double t[4] = {0.0, 0.0, 0.0, 0.0};
-    if (ix == 0 || iy == 0 || ix == N || iy == N) {
-      double x[2], gv[4];
-      bilinear_map(cs.corners, ix / (double)N, iy / (double)N, x);
-      q1_eval<2>(cs.q1coef, cs.q1shift, cs.q1iscale, x, gv);
-      const double sq = d64[g] * v64[4 * g];
+  // Dirichlet data phi~_i = D^1/2 g_i (BasisQ1 at the node) in a converged
+  // loop over the 4N boundary nodes (FP64 work in a divergent branch costs
+  // whole warp instructions); interior 0
+  const double invN = 1.0 / (double)N;
+  for (int k = tid; k < 4 * N; k += NT) {
+    int bx, by;
+    boundary_node(k, N, bx, by);
+    const int g = (by + 1) * P + bx + 1;
+    double x[2], gv[4], t[4];
+    bilinear_map(cs.corners, bx == N ? 1.0 : bx * invN, by == N ? 1.0 : by * invN, x);
+    q1_eval<2>(cs.q1coef, cs.q1shift, cs.q1iscale, x, gv);
+    const double sq = d64[g] * v64[4 * g];
 #pragma unroll
-      for (int r = 0; r < 4; ++r) t[r] = gv[r] * sq;
-    }
+    for (int r = 0; r < 4; ++r) t[r] = gv[r] * sq;
     st4(v64, g, t);
+  }
+  for (int k = tid; k < (N - 1) * (N - 1); k += NT) {
+    const double z4[4] = {0.0, 0.0, 0.0, 0.0};
+    st4(v64, (k / (N - 1) + 2) * P + k % (N - 1) + 2, z4);
   }
   if (tid == 0) {
     double m = 1e300;
@@ -808,6 +813,7 @@ msfem2d_kernel(const KernelParams p) {
   using L = Smem2D<NMAX>;
   constexpr int NW = NT / 32;
   constexpr int NPT = ((NMAX - 1) * (NMAX - 1) + NT - 1) / NT;  // interior nodes per thread
+  static_assert(4 * (NMAX - 2) <= NT, "the boundary-adjacent ring takes one node per thread");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double *c64 = reinterpret_cast<double *>(smem_raw + L::kC64);
   double *v64 = reinterpret_cast<double *>(smem_raw + L::kV64);
@@ -852,24 +858,38 @@ msfem2d_kernel(const KernelParams p) {
       gidx[j] = k < nI ? (1 + k / (N - 1) + 1) * P + (1 + k % (N - 1)) + 1 : -1;
       dloc[j] = gidx[j] >= 0 ? d64[gidx[j]] : 0.0;
     }
+    // b~ = -(A~ phi~)_I vanishes away from the boundary (phi~ is zero
+    // inside): one converged pass over the 4 (N - 2) boundary-adjacent nodes
+    // computes it, and the node owners pick it up from v64's (zero) interior
     double rr[NPT][4];   // FP64 residual (scaled)
     double bbp[4] = {0.0, 0.0, 0.0, 0.0};
-#pragma unroll
-    for (int j = 0; j < NPT; ++j) {
-#pragma unroll
-      for (int r = 0; r < 4; ++r) rr[j][r] = 0.0;
-      if (gidx[j] >= 0) {
-        double y[4];
-        stencil9<double>(c64, v64, gidx[j], P, y);
+    {
+      const int nring = N >= 3 ? 4 * (N - 2) : (N == 2 ? 1 : 0);
+      double bk[4] = {0.0, 0.0, 0.0, 0.0};
+      int gk = -1;
+      if (tid < nring) {
+        int rx, ry;
+        ring_node(tid, N, rx, ry);
+        gk = (ry + 1) * P + rx + 1;
+        stencil9<double>(c64, v64, gk, P, bk);
+        const double dk = d64[gk];
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
-          rr[j][r] = -y[r];
-          bbp[r] = fma(rr[j][r] * dloc[j], rr[j][r], bbp[r]);
+          bk[r] = -bk[r];
+          bbp[r] = (bk[r] * dk) * bk[r];
         }
       }
+      warp_partials<4>(bbp, red[1], warp, lane);
+      __syncthreads();  // every stencil read of v64 is done
+      if (gk >= 0) st4(v64, gk, bk);
+      __syncthreads();
+#pragma unroll
+      for (int j = 0; j < NPT; ++j) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) rr[j][r] = 0.0;
+        if (gidx[j] >= 0) ld4(v64, gidx[j], rr[j]);
+      }
     }
-    warp_partials<4>(bbp, red[1], warp, lane);
-    __syncthreads();
     if (warp == 0) {
       const double t = warp_finish<4>(red[1], NW, lane);
       if (lane < 4) {
