@@ -1203,6 +1203,56 @@ __device__ __forceinline__ void strip_apply(const float *__restrict__ buf, int g
   }
 }
 
+// y[0..1] += c x[0..1] and y[2..3] += c x[2..3] as two packed FP32 pair
+// FMAs (FFMA2): the four right-hand sides of a node in two instructions.
+// (Measured on the polynomial steps' stencil: 3 % faster with degree 5;
+// the same packing of the CG vector updates made the loop slower.)
+__device__ __forceinline__ void fma4_x2(float c, const float (&x)[4], float (&y)[4]) {
+  const float2 cc = make_float2(c, c);
+  const float2 a = __ffma2_rn(cc, make_float2(x[0], x[1]), make_float2(y[0], y[1]));
+  const float2 b = __ffma2_rn(cc, make_float2(x[2], x[3]), make_float2(y[2], y[3]));
+  y[0] = a.x; y[1] = a.y; y[2] = b.x; y[3] = b.y;
+}
+
+// strip_apply with packed pair FMAs (same operations, same rounding).
+template <int S>
+__device__ __forceinline__ void strip_apply_x2(const float *__restrict__ buf, int g0, int P, int ns,
+                                               const StripCoup<S> &c, const float (&x)[S][4], float (&y)[S][4]) {
+#pragma unroll
+  for (int s = 0; s < S; ++s)
+#pragma unroll
+    for (int r = 0; r < 4; ++r) y[s][r] = x[s][r];
+  if (ns <= 0) return;
+  float t4[4];
+  ld4(buf, g0 - P, t4);  // row below the strip
+  fma4_x2(c.cS[0], t4, y[0]);
+#pragma unroll
+  for (int s = 0; s < S; ++s) {
+    if (s < ns) {
+      if (s > 0) fma4_x2(c.cS[s], x[s - 1], y[s]);
+      if (s + 1 < ns) {
+        fma4_x2(c.cN[s], x[s + 1], y[s]);
+      } else {
+        ld4(buf, g0 + (s + 1) * P, t4);  // row above the strip
+        fma4_x2(c.cN[s], t4, y[s]);
+      }
+    }
+  }
+#pragma unroll
+  for (int u = -1; u <= S; ++u) {
+    if (u <= ns) {
+      ld4(buf, g0 + u * P - 1, t4);  // left column, row s0 + u
+      if (u >= 1 && u - 1 < ns) fma4_x2(c.cNW[u - 1], t4, y[u - 1]);
+      if (u >= 0 && u < ns) fma4_x2(c.cW[u], t4, y[u]);
+      if (u + 1 < ns && u + 1 < S) fma4_x2(c.cSW[u + 1], t4, y[u + 1]);
+      ld4(buf, g0 + u * P + 1, t4);  // right column, row s0 + u
+      if (u >= 1 && u - 1 < ns) fma4_x2(c.cNE[u - 1], t4, y[u - 1]);
+      if (u >= 0 && u < ns) fma4_x2(c.cE[u], t4, y[u]);
+      if (u + 1 < ns && u + 1 < S) fma4_x2(c.cSE[u + 1], t4, y[u + 1]);
+    }
+  }
+}
+
 template <int S>
 __device__ __forceinline__ void strip_store(float *__restrict__ buf, int g0, int P, int ns, const float (&x)[S][4]) {
 #pragma unroll
@@ -1641,7 +1691,7 @@ msfem2d_mixed_kernel(const KernelParams p) {
             strip_store<S>(bufk, g0, P, ns, zv);
             __syncthreads();
             float yv[S][4];
-            strip_apply<S>(bufk, g0, P, ns, cp, zv, yv);
+            strip_apply_x2<S>(bufk, g0, P, ns, cp, zv, yv);
 #pragma unroll
             for (int s = 0; s < S; ++s)
 #pragma unroll
@@ -1689,7 +1739,7 @@ msfem2d_mixed_kernel(const KernelParams p) {
           strip_store<S>(v32, g0, P, ns, pv);
           __syncthreads();
           float qv[S][4];
-          strip_apply<S>(v32, g0, P, ns, cp, pv, qv);
+          strip_apply_x2<S>(v32, g0, P, ns, cp, pv, qv);
           float sg[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
           for (int s = 0; s < S; ++s)
