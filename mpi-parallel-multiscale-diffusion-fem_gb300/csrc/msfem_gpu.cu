@@ -76,6 +76,10 @@ struct msfem_handle {
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // second stream of the size-class split (3D mixed, slab-cluster shape):
+  // the small cells run there beside the cluster launch, joined by events
+  cudaStream_t side_stream = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   // inputs staged from the host / internal scratch
   DevBuf corners, nfine, order, queue, qp, qpoff, warm, boff, modes, spheres, sgrid_start, sgrid_ids;
   DevBuf fqp, fqpoff;  // right-hand side tabulated at the Gauss points
@@ -750,7 +754,12 @@ int msfem_create(msfem_handle **handle, int device) {
   h->device = device;
   h->sm_count = prop.multiProcessorCount;
   if (cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess) {
+      cudaStreamCreateWithFlags(&h->side_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+    if (h->own_stream) cudaStreamDestroy(h->own_stream);
+    if (h->side_stream) cudaStreamDestroy(h->side_stream);
     delete h;
     return fail(MSFEM_ERR_CUDA, "stream/event creation failed");
   }
@@ -763,6 +772,7 @@ int msfem_destroy(msfem_handle *h) {
   if (!h) return MSFEM_OK;
   cudaSetDevice(h->device);
   cudaStreamSynchronize(h->stream);
+  cudaStreamSynchronize(h->side_stream);
   DevBuf *bufs[] = {&h->corners, &h->nfine, &h->order, &h->queue, &h->qp, &h->qpoff, &h->fqp, &h->fqpoff, &h->warm,
                     &h->boff, &h->modes, &h->spheres, &h->sgrid_start, &h->sgrid_ids,
                     &h->M, &h->F, &h->basis, &h->status, &h->iters, &h->relres, &h->refine,
@@ -771,7 +781,10 @@ int msfem_destroy(msfem_handle *h) {
   if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+  if (h->ev_join) cudaEventDestroy(h->ev_join);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
+  if (h->side_stream) cudaStreamDestroy(h->side_stream);
   delete h;
   return MSFEM_OK;
 }
@@ -1498,8 +1511,37 @@ int run_batch_impl(msfem_handle *h, const msfem_batch_desc *d, double *M, double
   p.basis = basis ? (double *)out_ptr(h->basis, basis, sizeof(double) * basis_total) : nullptr;
   if (!p.M || !p.F || !p.status || !p.iters || !p.rel_res || !p.refinements || (basis && !p.basis))
     return fail(MSFEM_ERR_OUT_OF_MEMORY, "device output allocation failed");
-  MSFEM_CUDA(h->queue.ensure(sizeof(unsigned int)));
+  MSFEM_CUDA(h->queue.ensure(2 * sizeof(unsigned int)));
   p.queue = h->queue.as<unsigned int>();
+
+  // ---- size-class split (3D mixed, slab-cluster shape, uneven N).  The
+  // cluster shape keeps a cell's inner CG in its CTAs' shared memory but
+  // occupies whole groups of 8 SMs and is slow on small cells; the cells with
+  // N > kSplitN (a prefix of the size-sorted order) go to the cluster launch,
+  // the rest to one CTA per cell (the 2-CTA/SM shape) on the side stream, on
+  // the SMs the clusters leave free.  Own queue counters, workspace slots
+  // after the clusters'.
+  constexpr int kSplitN = 16;
+  int n_large = nc;
+  const Launch *Ls = nullptr;
+  if (dim == 3 && mixed && L.cluster > 1 && d->n_fine_per_cell && nc > 0) {
+    n_large = 0;
+    for (int c = 0; c < nc; ++c) n_large += nf[c] > kSplitN ? 1 : 0;
+    for (const Launch &c : cands)
+      if (c.cluster == 1 && c.minb == 2 && c.nt == 256) Ls = &c;
+    if (!Ls || n_large == 0 || n_large == nc) {
+      Ls = nullptr;
+      n_large = nc;
+    }
+  }
+  const bool split = Ls != nullptr;
+  KernelParams ps = p;  // the small cells' launch
+  if (split) {
+    p.n_cells = n_large;
+    ps.n_cells = nc - n_large;
+    ps.order = p.order + n_large;
+    ps.queue = p.queue + 1;
+  }
 
   // ---- launch: persistent CTAs, size-sorted work queue
   if (L.smem > 0)
@@ -1508,12 +1550,14 @@ int run_batch_impl(msfem_handle *h, const msfem_batch_desc *d, double *M, double
   MSFEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, L.fn, L.nt, L.smem));
   if (per_sm < 1) return fail(MSFEM_ERR_UNSUPPORTED, "kernel does not fit on an SM");
   if (L.slot_bytes) per_sm = std::min(per_sm, L.minb);  // workspace slots per SM
-  int grid = std::max(1, std::min(nc, per_sm * h->sm_count));
+  const int ncl_cells = p.n_cells;
+  int grid = std::max(1, std::min(ncl_cells, per_sm * h->sm_count));
   int slots = grid;
   // thread-block clusters: as many co-resident clusters as the GPU holds,
   // one cell and one workspace slot per cluster
   cudaLaunchConfig_t ccfg = {};
   cudaLaunchAttribute cattr[1];
+  int ncl = 0;
   if (L.cluster > 1) {
     if (L.cluster > 8)
       MSFEM_CUDA(cudaFuncSetAttribute(L.fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
@@ -1527,22 +1571,56 @@ int run_batch_impl(msfem_handle *h, const msfem_batch_desc *d, double *M, double
     cattr[0].val.clusterDim.z = 1;
     ccfg.attrs = cattr;
     ccfg.numAttrs = 1;
-    int ncl = 0;
     MSFEM_CUDA(cudaOccupancyMaxActiveClusters(&ncl, L.fn, &ccfg));
     if (ncl < 1) return fail(MSFEM_ERR_UNSUPPORTED, "no cluster of this shape fits the GPU");
-    slots = std::max(1, std::min(nc, ncl));
+    slots = std::max(1, std::min(ncl_cells, ncl));
     grid = slots * L.cluster;
     ccfg.gridDim = dim3(grid);
   }
-  unsigned char *work = nullptr;
+  // the small cells' launch: one CTA per cell, two per SM, on the SMs left
+  // free by the clusters (at least one SM's worth; later CTAs find the queue
+  // drained)
+  int grid_s = 0;
+  if (split) {
+    int per_sm_s = 0;
+    MSFEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_s, Ls->fn, Ls->nt, Ls->smem));
+    if (per_sm_s < 1) return fail(MSFEM_ERR_UNSUPPORTED, "kernel does not fit on an SM");
+    per_sm_s = std::min(per_sm_s, Ls->minb);
+    const int free_sms = std::max(1, h->sm_count - ncl * L.cluster);
+    grid_s = std::max(1, std::min(nc - n_large, free_sms * per_sm_s));
+  }
+  unsigned char *work = nullptr, *work_s = nullptr;
   size_t slot_bytes = L.slot_bytes;
   if (slot_bytes) {
-    MSFEM_CUDA(h->work.ensure(slot_bytes * slots));
+    MSFEM_CUDA(h->work.ensure(slot_bytes * (slots + grid_s)));
     work = h->work.as<unsigned char>();
+    work_s = work + slot_bytes * slots;
   }
   auto launch_basis = [&](void **args) -> cudaError_t {
     if (L.cluster > 1) return cudaLaunchKernelExC(&ccfg, L.fn, args);
     return cudaLaunchKernel(L.fn, dim3(grid), dim3(L.nt), args, L.smem, h->stream);
+  };
+  // the whole launch sequence on h->stream (the small cells forked to the
+  // side stream and joined back)
+  auto launch_all = [&]() -> cudaError_t {
+    cudaError_t e = cudaMemsetAsync(p.queue, 0, 2 * sizeof(unsigned int), h->stream);
+    if (e != cudaSuccess || nc == 0) return e;
+    if (split) {
+      if ((e = cudaEventRecord(h->ev_fork, h->stream)) != cudaSuccess) return e;
+      if ((e = cudaStreamWaitEvent(h->side_stream, h->ev_fork, 0)) != cudaSuccess) return e;
+    }
+    void *args2[] = {&p};
+    void *args3[] = {&p, &work, &slot_bytes};
+    if ((e = launch_basis(slot_bytes ? args3 : args2)) != cudaSuccess) return e;
+    if (split) {
+      void *args_s[] = {&ps, &work_s, &slot_bytes};
+      if ((e = cudaLaunchKernel(Ls->fn, dim3(grid_s), dim3(Ls->nt), args_s, Ls->smem, h->side_stream)) !=
+          cudaSuccess)
+        return e;
+      if ((e = cudaEventRecord(h->ev_join, h->side_stream)) != cudaSuccess) return e;
+      if ((e = cudaStreamWaitEvent(h->stream, h->ev_join, 0)) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
   };
   // Device-resident asynchronous calls replay a CUDA graph of the
   // queue-reset + basis-kernel sequence; it is re-captured whenever the
@@ -1559,21 +1637,24 @@ int run_batch_impl(msfem_handle *h, const msfem_batch_desc *d, double *M, double
     key.append(reinterpret_cast<const char *>(&grid), sizeof(grid));
     key.append(reinterpret_cast<const char *>(&work), sizeof(work));
     key.append(reinterpret_cast<const char *>(&h->stream), sizeof(h->stream));
+    key.append(reinterpret_cast<const char *>(&split), sizeof(split));
+    if (split) {
+      key.append(reinterpret_cast<const char *>(&ps), sizeof(ps));
+      key.append(reinterpret_cast<const char *>(&Ls->fn), sizeof(Ls->fn));
+      key.append(reinterpret_cast<const char *>(&grid_s), sizeof(grid_s));
+    }
     if (key != h->graph_key || !h->graph_exec) {
       if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
       h->graph_exec = nullptr;
       h->graph_key.clear();
       cudaGraph_t graph = nullptr;
       MSFEM_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-      cudaError_t e1 = cudaMemsetAsync(p.queue, 0, sizeof(unsigned int), h->stream);
-      void *a2[] = {&p};
-      void *a3[] = {&p, &work, &slot_bytes};
-      cudaError_t e2 = launch_basis(slot_bytes ? a3 : a2);
-      cudaError_t e3 = cudaStreamEndCapture(h->stream, &graph);
-      if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
+      const cudaError_t e1 = launch_all();
+      const cudaError_t e3 = cudaStreamEndCapture(h->stream, &graph);
+      if (e1 != cudaSuccess || e3 != cudaSuccess) {
         if (graph) cudaGraphDestroy(graph);
         return fail(MSFEM_ERR_CUDA, std::string("graph capture failed: ") +
-                                        cudaGetErrorString(e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : e3)));
+                                        cudaGetErrorString(e1 != cudaSuccess ? e1 : e3));
       }
       const cudaError_t e4 = cudaGraphInstantiate(&h->graph_exec, graph, 0);
       cudaGraphDestroy(graph);
@@ -1585,16 +1666,11 @@ int run_batch_impl(msfem_handle *h, const msfem_batch_desc *d, double *M, double
       h->graph_captures++;
     }
     MSFEM_CUDA(cudaGraphLaunch(h->graph_exec, h->stream));
-    launches++;
+    launches += split ? 2 : 1;
     h->graph_launches++;
   } else {
-    MSFEM_CUDA(cudaMemsetAsync(p.queue, 0, sizeof(unsigned int), h->stream));
-    if (nc > 0) {
-      void *args2[] = {&p};
-      void *args3[] = {&p, &work, &slot_bytes};
-      MSFEM_CUDA(launch_basis(slot_bytes ? args3 : args2));
-      launches++;
-    }
+    MSFEM_CUDA(launch_all());
+    if (nc > 0) launches += split ? 2 : 1;
   }
   MSFEM_CUDA(cudaEventRecord(h->ev1, h->stream));
 

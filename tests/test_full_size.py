@@ -81,12 +81,79 @@ def test_every_compiled_3d_shape_at_sphere_field_sizes(pkg, oracle, engine, sphe
                                "inner_tol": 1e-6})
             got = engine.run(prob, precision=precision, tol=1e-12, want_basis=True)
             assert got["rc"] == 0 and np.all(got["status"] == 0), v
-            assert got["stats"]["kernel_launches"] == 2, v  # tabulation + one basis kernel
+            # tabulation + one basis kernel; the cluster shape of the mixed
+            # form splits the batch by size class (one more launch)
+            split = precision == "mixed" and v == probe["n_variants"] - 1
+            assert got["stats"]["kernel_launches"] == (3 if split else 2), v
             assert rel_err(got["M"], ref["M"]) < 1e-10, (v, rel_err(got["M"], ref["M"]))
             assert rel_err(got["F"], ref["F"]) < 1e-10, (v, rel_err(got["F"], ref["F"]))
             assert np.abs(got["basis"] - ref["basis"]).max() < 1e-9, v
     finally:
         engine.set_tuning({"dim": 3, "n_max": 24, "precision": prec, "variant": 0, "check_interval": 0,
+                           "inner_tol": 1e-6})
+
+
+@pytest.mark.parametrize("path", ["eager", "graph"])
+def test_size_class_split_against_oracle(pkg, oracle, engine, sphere_field, path):
+    """The mixed form with the thread-block-cluster shape on an uneven batch
+    splits it by size class: the N = 24 cell runs in the cluster launch, the
+    N = 16 and 8 cells in a one-CTA-per-cell launch on a second stream beside
+    it.  Eagerly (3 launches: tabulation and the two basis kernels), and from
+    device buffers through the CUDA graph (captured once, replayed once),
+    against the oracle."""
+    torch = pytest.importorskip("torch")
+    abi = pkg._abi
+    W = pkg.workloads
+    nf = sphere_field["n_fine_per_cell"]
+    cells = [int(np.flatnonzero(nf == v)[2]) for v in (24, 16, 8)]
+    prob = W.subset(sphere_field, cells)
+    ref = oracle.run(prob)
+    probe = engine.autotune(prob, precision="mixed", tol=1e-12, sample_cells=3)
+    slab = probe["n_variants"] - 1  # the cluster shape: the last compiled 3D mixed shape
+    engine.set_tuning({"dim": 3, "n_max": 24, "precision": 1, "variant": slab, "check_interval": 0,
+                       "inner_tol": 1e-6})
+    try:
+        if path == "eager":
+            got = engine.run(prob, precision="mixed", tol=1e-12)
+            assert got["rc"] == 0 and np.all(got["status"] == 0)
+            assert got["stats"]["kernel_launches"] == 3
+            runs = [(got["M"], got["F"])]
+        else:
+            n = len(cells)
+            nf_d = torch.from_numpy(np.ascontiguousarray(prob["n_fine_per_cell"], dtype=np.int32)).cuda()
+            corners_d = torch.from_numpy(np.ascontiguousarray(prob["corners"])).cuda()
+            tab_d = torch.from_numpy(engine.tabulate(prob, 1)).cuda()
+            d = abi.BatchDesc()
+            d.dim, d.n_cells, d.n_fine = 3, n, 24
+            d.precision = abi.PREC_MIXED
+            d.corners, d.n_fine_per_cell = corners_d.data_ptr(), nf_d.data_ptr()
+            d.coef.kind, d.coef.ncomp, d.coef.qp_values = abi.COEF_TABULATED, 1, tab_d.data_ptr()
+            d.f_value, d.tol, d.maxit, d.memory = prob["f_value"], 1e-12, 1000, abi.MEM_DEVICE
+            M = torch.empty((n, 8, 8), dtype=torch.float64, device="cuda")
+            F = torch.empty((n, 8), dtype=torch.float64, device="cuda")
+            st = torch.empty(n, dtype=torch.int32, device="cuda")
+            it = torch.empty((n, 8), dtype=torch.int32, device="cuda")
+            engine.set_stream(None)  # the handle's own stream: graphs are used
+            cap0, rep0 = engine.graph_info()
+            runs = []
+            for call in range(2):
+                M.fill_(float("nan"))
+                F.fill_(float("nan"))
+                st.fill_(-7)
+                torch.cuda.synchronize()
+                rc, s = engine.run_desc(d, M.data_ptr(), F.data_ptr(), None, st.data_ptr(), it.data_ptr(),
+                                        stats=False)
+                assert rc == abi.OK and s is None
+                torch.cuda.synchronize()
+                assert np.all(st.cpu().numpy() == abi.CELL_CONVERGED), call
+                runs.append((M.cpu().numpy(), F.cpu().numpy()))
+            cap, rep = engine.graph_info()
+            assert (cap - cap0, rep - rep0) == (1, 2)
+        for M, F in runs:
+            assert rel_err(M, ref["M"]) < 1e-10, rel_err(M, ref["M"])
+            assert rel_err(F, ref["F"]) < 1e-10, rel_err(F, ref["F"])
+    finally:
+        engine.set_tuning({"dim": 3, "n_max": 24, "precision": 1, "variant": 0, "check_interval": 0,
                            "inner_tol": 1e-6})
 
 
