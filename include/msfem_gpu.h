@@ -288,6 +288,8 @@ typedef struct msfem_tuning {
                                (0 = Jacobi-scaled CG) */
   int32_t cluster_ctas;     /* output: CTAs of a thread-block cluster sharing one cell
                                (3D cluster shapes), 1 = one CTA per cell */
+  int32_t coarse_spacing;   /* output: fine cells per coarse-grid interval of that shape's
+                               two-level inner preconditioner (MIXED 2D), 0 = none */
 } msfem_tuning;
 
 /* Time every compiled shape and parameter choice for desc's key on a prefix

@@ -129,6 +129,7 @@ class Tuning(ctypes.Structure):
         ("cheb_ratio", ctypes.c_float),
         ("poly_degree", ctypes.c_int32),
         ("cluster_ctas", ctypes.c_int32),
+        ("coarse_spacing", ctypes.c_int32),
     ]
 
     def as_dict(self):

@@ -10,13 +10,15 @@ template <int NMAX, int NT>
 Launch make2d() {
   return Launch{(const void *)msfem2d_kernel<NMAX, NT>, NT, Smem2D<NMAX>::bytes(false), 0, 2, 0, 0};
 }
-template <int NMAX, int NT, int S, int MINB, int M = 0>
+template <int NMAX, int NT, int S, int MINB, int M = 0, int CH = 0>
 Launch make2d_mixed() {
   using L = Smem2D<NMAX>;
   // the polynomial-preconditioned form needs a second exchange buffer unless
-  // it runs two CTAs per SM (one buffer, one more barrier per Chebyshev step)
-  return Launch{(const void *)msfem2d_mixed_kernel<NMAX, NT, S, MINB, M>, NT,
-                (M > 0 && MINB < 2) ? L::kEndCheb : L::bytes(true), S, MINB, 0, M > 0 ? M - 1 : 0};
+  // it runs two CTAs per SM (one buffer, one more barrier per Chebyshev step);
+  // the two-level form adds its coarse-grid arrays
+  const size_t smem = CH > 0 ? Coarse2D<NMAX, CH>::kEnd : (M > 0 && MINB < 2) ? L::kEndCheb : L::bytes(true);
+  return Launch{(const void *)msfem2d_mixed_kernel<NMAX, NT, S, MINB, M, CH>, NT, smem, S, MINB, 0,
+                M > 0 ? M - 1 : 0, 1, CH};
 }
 
 }  // namespace
@@ -32,7 +34,10 @@ std::vector<Launch> candidates_2d(int nmax, bool mixed) {
     return {make2d_mixed<32, 256, 4, 2>(), make2d_mixed<32, 256, 4, 1>(), make2d_mixed<32, 512, 2, 1>(),
             // polynomial-preconditioned inner CG (degree M - 1 Chebyshev)
             make2d_mixed<32, 512, 2, 1, 4>(), make2d_mixed<32, 512, 2, 1, 6>(), make2d_mixed<32, 256, 4, 1, 4>(),
-            make2d_mixed<32, 256, 4, 1, 6>(), make2d_mixed<32, 256, 4, 2, 4>(), make2d_mixed<32, 256, 4, 2, 6>()};
+            make2d_mixed<32, 256, 4, 1, 6>(), make2d_mixed<32, 256, 4, 2, 4>(), make2d_mixed<32, 256, 4, 2, 6>(),
+            // two-level V-cycle: Chebyshev smoothing of degree M - 1 around a
+            // Galerkin coarse-grid correction of spacing 4
+            make2d_mixed<32, 256, 4, 1, 3, 4>(), make2d_mixed<32, 256, 4, 1, 4, 4>()};
   return {make2d<32, 256>()};
 }
 

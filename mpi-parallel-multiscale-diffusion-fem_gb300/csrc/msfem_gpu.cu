@@ -1755,6 +1755,7 @@ void fill_tuning(const Tune &t, int dim, int nmax, int precision, msfem_tuning *
     out->ctas_per_sm = c[t.variant].minb;
     out->poly_degree = c[t.variant].poly;
     out->cluster_ctas = c[t.variant].cluster;
+    out->coarse_spacing = c[t.variant].coarse;
   }
   out->cheb_ratio = t.cheb_ratio;
   out->check_interval = t.check_interval;
@@ -1917,7 +1918,11 @@ int msfem_autotune(msfem_handle *h, const msfem_batch_desc *d, int32_t sample_ce
     if (mixed) {
       for (float it : {1e-4f, 1e-5f, 1e-6f, 1e-7f}) {
         if (cands[v].poly > 0) {
-          for (float ratio : {10.0f, 30.0f, 100.0f}) {
+          // two-level shapes smooth with a narrower interval than the
+          // polynomial preconditioner alone
+          const std::vector<float> ratios = cands[v].coarse > 0 ? std::vector<float>{10.0f, 15.0f, 25.0f}
+                                                                 : std::vector<float>{10.0f, 30.0f, 100.0f};
+          for (float ratio : ratios) {
             Tune t;
             t.variant = v;
             t.inner_tol = it;

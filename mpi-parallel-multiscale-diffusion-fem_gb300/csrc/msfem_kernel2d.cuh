@@ -50,6 +50,29 @@ struct Smem2D {
   static_assert(kV64 % 16 == 0 && kV32 % 16 == 0, "vector alignment");
 };
 
+// Coarse-grid arrays of the two-level preconditioner (mixed form), after the
+// second FP32 exchange buffer.  Coarse spacing CH fine cells, so at most
+// NC = NMAX / CH coarse intervals and NI = (NC - 1)^2 interior coarse nodes:
+//   ub  [NC][2][32] float4  row-block partial restrictions (lower / upper
+//                           coarse row, by fine column); during the set-up the
+//                           band Cholesky factor of Ac
+//   rc  [NI] float4         restricted residual, 4 RHS
+//   ec  [NC+1][NC+1] float4 coarse correction with a zero boundary ring
+//   a0  [NI][NI] float      set-up scratch: row j = column j of L^-1 (Ac = L L^T)
+//   a1  [NI][NI] float      the Galerkin coarse matrix Ac, then Ac^-1 = L^-T L^-1
+template <int NMAX, int CH>
+struct Coarse2D {
+  using L = Smem2D<NMAX>;
+  static constexpr int NC = CH > 0 ? NMAX / CH : 2;
+  static constexpr int NI = (NC - 1) * (NC - 1);
+  static constexpr size_t kUB = L::kEndCheb;
+  static constexpr size_t kRC = L::al(kUB + 16 * 2 * 32 * NC);
+  static constexpr size_t kEC = L::al(kRC + 16 * NI);
+  static constexpr size_t kA0 = L::al(kEC + 16 * (NC + 1) * (NC + 1));
+  static constexpr size_t kA1 = L::al(kA0 + sizeof(float) * NI * NI);
+  static constexpr size_t kEnd = L::al(kA1 + sizeof(float) * NI * NI);
+};
+
 __device__ __forceinline__ void ld4(const double *__restrict__ v, int g, double (&t)[4]) {
   const double2 a = *reinterpret_cast<const double2 *>(v + 4 * g);
   const double2 b = *reinterpret_cast<const double2 *>(v + 4 * g + 2);
@@ -1284,16 +1307,28 @@ __device__ __forceinline__ void block_sum_f(float (&v)[K], float *red, int warp,
 // s0 = 1 + S (t / (N-1)): the strip's own search-direction values stay in
 // registers, only its two neighbour columns and two halo rows come from
 // shared memory.
+//
+// Inner preconditioner: M = 0 Jacobi scaling only; M > 0 a Chebyshev
+// polynomial of degree M - 1 on the scaled operator; CH > 0 (with M > 0) a
+// symmetric two-level V-cycle: Chebyshev smoothing of degree M - 1 before and
+// after a Galerkin coarse-grid correction on the bilinear coarse space of
+// spacing CH fine cells (used where CH divides N and the coarse grid has
+// interior nodes; other cells take the smoother alone).
 // ===========================================================================
-template <int NMAX, int NT, int S, int MINB, int M>
+template <int NMAX, int NT, int S, int MINB, int M, int CH = 0>
 __global__ void __launch_bounds__(NT, MINB)
 msfem2d_mixed_kernel(const KernelParams p) {
   using L = Smem2D<NMAX>;
+  using C = Coarse2D<NMAX, CH>;
   constexpr int NW = NT / 32;
   // threads per row-block of strips: the interior columns rounded up to a
   // multiple of 8 lanes (one quarter-warp of 16-byte accesses)
   constexpr int kSlots = (NMAX - 1 + 7) / 8 * 8;
   static_assert(kSlots * ((NMAX - 1 + S - 1) / S) <= NT, "strips must cover the interior");
+  // the coarse grid's rows are the strips' row-blocks and its columns fall
+  // within one warp of strips; two exchange buffers
+  static_assert(CH == 0 || (CH == S && kSlots == 32 && MINB == 1 && M >= 2), "two-level shape");
+  static_assert(CH == 0 || 4 * C::NI <= NT, "four threads per coarse node in the coarse solve");
   static_assert(NW * 32 * sizeof(double) <= 16 * L::G, "epilogue partials fit in v32");
   static_assert(4 * (NMAX - 2) <= NT, "the boundary-adjacent ring takes one node per thread");
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1460,6 +1495,255 @@ msfem2d_mixed_kernel(const KernelParams p) {
         cheb_c1[k] = rho_k * rho_prev;
         cheb_c2[k] = 2.0f * rho_k / delta;
         rho_prev = rho_k;
+      }
+    }
+
+    // ---- two-level preconditioner (CH > 0): coarse grid of ncg intervals of
+    // CH fine cells; coarse row j at fine row CH j is the boundary between
+    // strip row-blocks j - 1 and j, so each strip sees exactly coarse rows
+    // blk and blk + 1, with bilinear weights (CH - 1 - s) / CH and (s + 1) / CH
+    const int ncg = (CH > 0 && N % (CH > 0 ? CH : 1) == 0) ? N / (CH > 0 ? CH : 1) : 0;
+    const bool coarse = CH > 0 && ncg >= 2;
+    const int nI = coarse ? (ncg - 1) * (ncg - 1) : 0;
+    float4 *ub = reinterpret_cast<float4 *>(smem_raw + C::kUB);
+    float4 *rcs = reinterpret_cast<float4 *>(smem_raw + C::kRC);
+    float4 *ecz = reinterpret_cast<float4 *>(smem_raw + C::kEC);
+    const float *Aci = reinterpret_cast<const float *>(smem_raw + C::kA0);
+    // D^1/2 of the strip (the coarse space in scaled variables is D^1/2 P)
+    float sq[S];
+#pragma unroll
+    for (int s = 0; s < S; ++s) sq[s] = sown[s] > 0.0f ? 1.0f / sown[s] : 0.0f;
+    // bilinear x weights of the strip's column: coarse columns cxl, cxl + 1
+    const int cxl = CH > 0 ? ix / (CH > 0 ? CH : 1) : 0;
+    const float wxh = CH > 0 ? (float)(ix - CH * cxl) * (1.0f / (CH > 0 ? CH : 1)) : 0.0f, wxl = 1.0f - wxh;
+    // one stencil pass y = A~ x through the exchange buffers v32 / v32b in
+    // turn: one barrier per pass, since a buffer is written again only after
+    // the barrier that follows every read of it
+    int bsel = 0;
+    auto pass = [&](const float (&x)[S][4], float (&y)[S][4]) {
+      float *bk = bsel ? v32b : v32;
+      bsel ^= 1;
+      strip_store<S>(bk, g0, P, ns, x);
+      __syncthreads();
+      strip_apply_x2<S>(bk, g0, P, ns, cp, x, y);
+    };
+    // rcs = (D^1/2 P)^T e: each strip folds its rows onto its two coarse
+    // rows, then one thread per coarse node sums the 2 CH - 1 columns of
+    // the two row-blocks next to it (measured faster than a shuffle window
+    // sum inside each row-block, whose partials the coarse solve would
+    // then have to combine)
+    auto restrict_c = [&](const float (&e)[S][4], bool closing_barrier = true) {
+      if (own) {
+        float lo[4] = {0.f, 0.f, 0.f, 0.f}, hi[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+          const float wl = (float)(CH - 1 - s) * (1.0f / (CH > 0 ? CH : 1)) * sq[s];
+          const float wh = (float)(s + 1) * (1.0f / (CH > 0 ? CH : 1)) * sq[s];
+#pragma unroll
+          for (int r = 0; r < 4; ++r) {
+            lo[r] = fmaf(wl, e[s][r], lo[r]);
+            hi[r] = fmaf(wh, e[s][r], hi[r]);
+          }
+        }
+        ub[(2 * blk) * 32 + col] = make_float4(lo[0], lo[1], lo[2], lo[3]);
+        ub[(2 * blk + 1) * 32 + col] = make_float4(hi[0], hi[1], hi[2], hi[3]);
+      }
+      __syncthreads();
+      if (tid < nI) {
+        const int cy = 1 + tid / (ncg - 1), cx = 1 + tid % (ncg - 1);
+        float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int d = 1 - CH; d <= CH - 1; ++d) {
+          const float w = (float)(CH - (d < 0 ? -d : d)) * (1.0f / (CH > 0 ? CH : 1));
+          const int c = CH * cx + d - 1;  // lane of fine column CH cx + d
+          const float4 u0 = ub[(2 * cy) * 32 + c], u1 = ub[(2 * cy - 1) * 32 + c];
+          a.x = fmaf(w, u0.x + u1.x, a.x);
+          a.y = fmaf(w, u0.y + u1.y, a.y);
+          a.z = fmaf(w, u0.z + u1.z, a.z);
+          a.w = fmaf(w, u0.w + u1.w, a.w);
+        }
+        rcs[tid] = a;
+      }
+      if (closing_barrier) __syncthreads();  // uniform argument
+    };
+    // cr = D^1/2 P Ac^-1 rcs: four threads per coarse node (a quarter of the
+    // dense row each), then bilinear prolongation from the strip's corners
+    auto coarse_solve = [&](float (&cr)[S][4]) {
+      if (tid < ((4 * nI + 31) & ~31)) {  // whole warps (shuffles below)
+        const int i = tid >> 2, q = tid & 3;
+        float a[4] = {0.f, 0.f, 0.f, 0.f};
+        if (i < nI)
+          for (int j = q; j < nI; j += 4) {
+            const float w = Aci[i * nI + j];
+            const float4 v = rcs[j];
+            a[0] = fmaf(w, v.x, a[0]);
+            a[1] = fmaf(w, v.y, a[1]);
+            a[2] = fmaf(w, v.z, a[2]);
+            a[3] = fmaf(w, v.w, a[3]);
+          }
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          a[r] += __shfl_xor_sync(0xffffffffu, a[r], 1);
+          a[r] += __shfl_xor_sync(0xffffffffu, a[r], 2);
+        }
+        if (q == 0 && i < nI)
+          ecz[(1 + i / (ncg - 1)) * (ncg + 1) + 1 + i % (ncg - 1)] = make_float4(a[0], a[1], a[2], a[3]);
+      }
+      __syncthreads();
+      float bo[4] = {0.f, 0.f, 0.f, 0.f}, to[4] = {0.f, 0.f, 0.f, 0.f};
+      if (own) {
+        const float4 e00 = ecz[blk * (ncg + 1) + cxl], e01 = ecz[blk * (ncg + 1) + cxl + 1];
+        const float4 e10 = ecz[(blk + 1) * (ncg + 1) + cxl], e11 = ecz[(blk + 1) * (ncg + 1) + cxl + 1];
+        bo[0] = wxl * e00.x + wxh * e01.x; bo[1] = wxl * e00.y + wxh * e01.y;
+        bo[2] = wxl * e00.z + wxh * e01.z; bo[3] = wxl * e00.w + wxh * e01.w;
+        to[0] = wxl * e10.x + wxh * e11.x; to[1] = wxl * e10.y + wxh * e11.y;
+        to[2] = wxl * e10.z + wxh * e11.z; to[3] = wxl * e10.w + wxh * e11.w;
+      }
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        const float wh = (float)(s + 1) * (1.0f / (CH > 0 ? CH : 1)), wl = 1.0f - wh;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) cr[s][r] = sq[s] * fmaf(wl, bo[r], wh * to[r]);
+      }
+    };
+    if constexpr (CH > 0) {
+      if (coarse) {  // uniform over the CTA
+        float *a0 = reinterpret_cast<float *>(smem_raw + C::kA0);
+        float *a1 = reinterpret_cast<float *>(smem_raw + C::kA1);
+        for (int i = tid; i < nI * nI; i += NT) a1[i] = 0.0f;
+        for (int i = tid; i < (ncg + 1) * (ncg + 1); i += NT) ecz[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        __syncthreads();
+        // Galerkin Ac = (D^1/2 P)^T A~ (D^1/2 P) by probing: coarse node J
+        // has colour (jx mod 3) + 3 (jy mod 3), and one stencil pass over the
+        // sum of the coarse functions of 4 colours (one per RHS lane) gives,
+        // restricted to node I, the entry of the colour's one J next to I
+#pragma unroll 1
+        for (int pp = 0; pp < 3; ++pp) {
+          float v[S][4];
+#pragma unroll
+          for (int s = 0; s < S; ++s)
+#pragma unroll
+            for (int r = 0; r < 4; ++r) v[s][r] = 0.0f;
+          if (own) {
+#pragma unroll
+            for (int b = 0; b < 2; ++b)
+#pragma unroll
+              for (int a = 0; a < 2; ++a) {
+                const int jx = cxl + a, jy = blk + b;
+                if (jx < 1 || jx > ncg - 1 || jy < 1 || jy > ncg - 1) continue;
+                const int colour = jx % 3 + 3 * (jy % 3) - 4 * pp;
+                const float wx = a ? wxh : wxl;
+#pragma unroll
+                for (int s = 0; s < S; ++s) {
+                  const float wy = (float)(b ? s + 1 : CH - 1 - s) * (1.0f / CH);
+#pragma unroll
+                  for (int r = 0; r < 4; ++r)
+                    if (colour == r) v[s][r] = fmaf(sq[s] * wx, wy, v[s][r]);
+                }
+              }
+          }
+          float y[S][4];
+          pass(v, y);
+          restrict_c(y, false);  // rcs[tid] is read back by the thread that wrote it
+          if (tid < nI) {
+            const int Ix = 1 + tid % (ncg - 1), Iy = 1 + tid / (ncg - 1);
+            const float4 rr = rcs[tid];
+            const float rv4[4] = {rr.x, rr.y, rr.z, rr.w};
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+              const int c = 4 * pp + r;
+              if (c >= 9) continue;
+              const int jx = Ix - 1 + ((c % 3 - (Ix - 1) % 3 + 3) % 3);
+              const int jy = Iy - 1 + ((c / 3 - (Iy - 1) % 3 + 3) % 3);
+              if (jx >= 1 && jx <= ncg - 1 && jy >= 1 && jy <= ncg - 1)
+                a1[tid * nI + (jy - 1) * (ncg - 1) + jx - 1] = rv4[r];
+            }
+          }
+        }
+        __syncthreads();
+        // Ac^-1 without block barriers per pivot.  In the lexicographic
+        // coarse numbering Ac is banded (bandwidth ncg <= W = NC), so warp 0
+        // factors Ac = L L^T left-looking (lane p computes row k + p of
+        // column k; warp-synchronous; measured faster than keeping the band
+        // rows in registers and moving them by shuffles), then thread j
+        // solves L L^T x = e_j for column j of the inverse.  Band storage
+        // Lb[i][W - q] = L[i][i - q] and 1 / L[i][i] live in ub (free here);
+        // the symmetrised probe is read from a1.
+        constexpr int W = C::NC;
+        float *__restrict__ Lb = reinterpret_cast<float *>(ub);
+        float *__restrict__ invd = Lb + C::NI * (W + 1);
+        const float *__restrict__ A1 = a1;
+        if (warp == 0) {
+#pragma unroll 1
+          for (int k = 0; k < nI; ++k) {
+            const int i = k + lane;
+            float sp = 0.0f;
+            if (lane <= W && i < nI) {
+              sp = 0.5f * (A1[i * nI + k] + A1[k * nI + i]);
+#pragma unroll
+              for (int q = 1; q <= W; ++q)
+                if (q <= W - lane && k - q >= 0) sp = fmaf(-Lb[i * (W + 1) + W - lane - q], Lb[k * (W + 1) + W - q], sp);
+            }
+            const float piv = __shfl_sync(0xffffffffu, sp, 0);
+            const float id = piv > 0.0f ? rsqrtf(piv) : 0.0f;  // a lost pivot drops that coarse mode
+            if (lane == 0) {
+              Lb[k * (W + 1) + W] = piv * id;
+              invd[k] = id;
+            } else if (lane <= W && i < nI) {
+              Lb[i * (W + 1) + W - lane] = sp * id;
+            }
+            __syncwarp();
+          }
+        }
+        __syncthreads();
+        if (tid < nI) {
+          // column j of X = L^-1 by forward substitution in blocks of W
+          // steps (the W-value window of the recurrence stays in
+          // registers), stored as row j of a0 (measured faster than
+          // computing the rows of X inside the factorisation loop)
+          float *__restrict__ row = a0 + tid * nI;
+          float win[W];
+#pragma unroll
+          for (int q = 0; q < W; ++q) win[q] = 0.0f;
+#pragma unroll 1
+          for (int kb = 0; kb < nI; kb += W) {
+#pragma unroll
+            for (int u = 0; u < W; ++u) {
+              const int k = kb + u;
+              float yk = 0.0f;
+              if (k < nI) {
+                float s = k == tid ? 1.0f : 0.0f;
+#pragma unroll
+                for (int q = W; q >= 1; --q)  // newest term last: shorter dependency chain
+                  if (k - q >= 0) s = fmaf(-Lb[k * (W + 1) + W - q], win[(u - q + W) % W], s);
+                yk = s * invd[k];
+              }
+              win[u] = yk;
+            }
+#pragma unroll
+            for (int u = 0; u < W; ++u)
+              if (kb + u < nI) row[kb + u] = win[u];
+          }
+        }
+        __syncthreads();
+        // Ac^-1 = X^T X into a1 (the probe is no longer needed): entry (i, j),
+        // i >= j, is the dot product of rows i and j of a0 from column i on
+        {
+          const int ntri = nI * (nI + 1) / 2;
+          for (int e = tid; e < ntri; e += NT) {
+            int i = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
+            while (i > 0 && i * (i + 1) / 2 > e) --i;
+            while ((i + 1) * (i + 2) / 2 <= e) ++i;
+            const int j = e - i * (i + 1) / 2;
+            const float *xi = a0 + i * nI, *xj = a0 + j * nI;
+            float acc = 0.0f;
+            for (int k = i; k < nI; ++k) acc = fmaf(xi[k], xj[k], acc);
+            a1[i * nI + j] = acc;
+            a1[j * nI + i] = acc;
+          }
+        }
+        __syncthreads();
+        Aci = a1;
       }
     }
 
@@ -1673,32 +1957,90 @@ msfem2d_mixed_kernel(const KernelParams p) {
             rv[s][r] = s < ns ? (float)r64[s][r] * sown[s] * act[r] : 0.0f;
             dv[s][r] = 0.0f;
           }
-        auto apply_prec = [&]() {
+        // Chebyshev smoothing in residual form: zv += p(A~) e, e tracking the
+        // residual of the added part (its last update only when need_res)
+        auto smooth = [&](float (&e)[S][4], bool need_res) {
+          float dd[S][4], yv[S][4];
 #pragma unroll
           for (int s = 0; s < S; ++s)
 #pragma unroll
             for (int r = 0; r < 4; ++r) {
-              zv[s][r] = rv[s][r] * cheb_inv_theta;
-              ddv[s][r] = zv[s][r];
+              dd[s][r] = e[s][r] * cheb_inv_theta;
+              zv[s][r] += dd[s][r];
             }
 #pragma unroll
           for (int k = 1; k < M; ++k) {
-            // two buffers alternate (one barrier per step); with one buffer
-            // (MINB >= 2, less shared memory) a second barrier orders the
-            // reads of step k before the writes of step k + 1
-            float *bufk = (MINB >= 2 || (k & 1) == 0) ? v32 : v32b;
-            if (MINB >= 2 && k > 1) __syncthreads();
-            strip_store<S>(bufk, g0, P, ns, zv);
-            __syncthreads();
-            float yv[S][4];
-            strip_apply_x2<S>(bufk, g0, P, ns, cp, zv, yv);
+            pass(dd, yv);
 #pragma unroll
             for (int s = 0; s < S; ++s)
 #pragma unroll
               for (int r = 0; r < 4; ++r) {
-                ddv[s][r] = fmaf(cheb_c1[k], ddv[s][r], cheb_c2[k] * (rv[s][r] - yv[s][r]));
-                zv[s][r] += ddv[s][r];
+                e[s][r] -= yv[s][r];
+                dd[s][r] = fmaf(cheb_c1[k], dd[s][r], cheb_c2[k] * e[s][r]);
+                zv[s][r] += dd[s][r];
               }
+          }
+          if (need_res) {
+            pass(dd, yv);
+#pragma unroll
+            for (int s = 0; s < S; ++s)
+#pragma unroll
+              for (int r = 0; r < 4; ++r) e[s][r] -= yv[s][r];
+          }
+        };
+        auto apply_prec = [&]() {
+          if constexpr (CH > 0) {
+            // z = B r: pre-smoothing, coarse correction, post-smoothing
+            float e[S][4];
+#pragma unroll
+            for (int s = 0; s < S; ++s)
+#pragma unroll
+              for (int r = 0; r < 4; ++r) {
+                e[s][r] = rv[s][r];
+                zv[s][r] = 0.0f;
+              }
+            if (coarse) {
+              smooth(e, true);
+              float cr[S][4], yv[S][4];
+              restrict_c(e);
+              coarse_solve(cr);
+              pass(cr, yv);
+#pragma unroll
+              for (int s = 0; s < S; ++s)
+#pragma unroll
+                for (int r = 0; r < 4; ++r) {
+                  zv[s][r] += cr[s][r];
+                  e[s][r] -= yv[s][r];
+                }
+            }
+            smooth(e, false);
+          } else {
+#pragma unroll
+            for (int s = 0; s < S; ++s)
+#pragma unroll
+              for (int r = 0; r < 4; ++r) {
+                zv[s][r] = rv[s][r] * cheb_inv_theta;
+                ddv[s][r] = zv[s][r];
+              }
+#pragma unroll
+            for (int k = 1; k < M; ++k) {
+              // two buffers alternate (one barrier per step); with one buffer
+              // (MINB >= 2, less shared memory) a second barrier orders the
+              // reads of step k before the writes of step k + 1
+              float *bufk = (MINB >= 2 || (k & 1) == 0) ? v32 : v32b;
+              if (MINB >= 2 && k > 1) __syncthreads();
+              strip_store<S>(bufk, g0, P, ns, zv);
+              __syncthreads();
+              float yv[S][4];
+              strip_apply_x2<S>(bufk, g0, P, ns, cp, zv, yv);
+#pragma unroll
+              for (int s = 0; s < S; ++s)
+#pragma unroll
+                for (int r = 0; r < 4; ++r) {
+                  ddv[s][r] = fmaf(cheb_c1[k], ddv[s][r], cheb_c2[k] * (rv[s][r] - yv[s][r]));
+                  zv[s][r] += ddv[s][r];
+                }
+            }
           }
         };
         auto dots_rz_rr = [&](float (&out)[8]) {
@@ -1735,11 +2077,15 @@ msfem2d_mixed_kernel(const KernelParams p) {
         for (;;) {
           if (!(iact[0] || iact[1] || iact[2] || iact[3]) || iit >= p.inner_maxit) break;
           ++iit;
-          // q = A~ p (p exchanged through v32)
-          strip_store<S>(v32, g0, P, ns, pv);
-          __syncthreads();
+          // q = A~ p (p exchanged through v32; the two-level form alternates)
           float qv[S][4];
-          strip_apply_x2<S>(v32, g0, P, ns, cp, pv, qv);
+          if constexpr (CH > 0) {
+            pass(pv, qv);
+          } else {
+            strip_store<S>(v32, g0, P, ns, pv);
+            __syncthreads();
+            strip_apply_x2<S>(v32, g0, P, ns, cp, pv, qv);
+          }
           float sg[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
           for (int s = 0; s < S; ++s)

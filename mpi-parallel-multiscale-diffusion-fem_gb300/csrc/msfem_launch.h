@@ -24,6 +24,7 @@ struct Launch {
   size_t slot_bytes; // per-CTA (per-cluster) global workspace (3D kernels), 0 = none
   int poly;          // degree of the inner polynomial preconditioner (mixed 2D), 0 = none
   int cluster = 1;   // CTAs per thread-block cluster sharing one cell (3D), 1 = none
+  int coarse = 0;    // coarse-grid spacing of the two-level inner preconditioner (mixed 2D), 0 = none
 };
 
 // Compiled launch shapes per N class and precision; index 0 is the default.
