@@ -65,11 +65,23 @@ def flops_per_solve_iter_3d(N):
     return 2 * (3 * N - 5) ** 3 + 11 * (N - 1) ** 3
 
 
-def inner_flops_per_iter(N, poly):
-    """Inner FP32 iteration of the mixed 2D form with a polynomial
-    preconditioner of degree `poly` (poly + 1 stencils, two dot-product
-    pairs and the vector updates): (poly + 1) 2 nnz(A_II) + (11 + 4 poly) n_I."""
-    return (poly + 1) * 2 * (3 * N - 5) ** 2 + (11 + 4 * poly) * (N - 1) ** 2
+def inner_flops_per_iter(N, poly, coarse=0):
+    """Inner FP32 iteration of the mixed 2D form, per right-hand side.
+
+    Polynomial preconditioner of degree `poly` (poly + 1 stencils, two
+    dot-product pairs and the vector updates): (poly + 1) 2 nnz(A_II) +
+    (11 + 4 poly) n_I.  Two-level V-cycle (`coarse` = coarse spacing > 0,
+    smoothing degree poly = M - 1): 2M + 1 stencils (search direction, M
+    pre-smoothing, the coarse correction's, M - 1 post-smoothing), 10 M + 22
+    vector operations per node, the restriction and prolongation
+    (28 per coarse node) and the dense coarse solve 2 n_c^2, n_c the
+    interior coarse nodes."""
+    nnz, n_i = (3 * N - 5) ** 2, (N - 1) ** 2
+    if coarse and N % coarse == 0 and N // coarse >= 2:
+        m = poly + 1
+        n_c = (N // coarse - 1) ** 2
+        return (2 * m + 1) * 2 * nnz + (10 * m + 22) * n_i + 2 * n_c * n_c + 28 * n_c
+    return (poly + 1) * 2 * nnz + (11 + 4 * poly) * n_i
 
 
 def flops_one_off_per_cell(N):
@@ -516,7 +528,8 @@ def main():
         }
         # achieved FP32 work of the inner loop (algorithmic flops per inner
         # iteration times the iterations executed) over the whole step time
-        fl32 = stmx["iterations_total"] * inner_flops_per_iter(N_FINE, int(tunemx.get("poly_degree", 0)))
+        fl32 = stmx["iterations_total"] * inner_flops_per_iter(N_FINE, int(tunemx.get("poly_degree", 0)),
+                                                              int(tunemx.get("coarse_spacing", 0)))
         line["mixed"]["inner_fp32_tflops"] = fl32 / (msmx * 1e-3) / 1e12
         line["mixed"]["inner_fp32_frac_of_measured_peak"] = line["mixed"]["inner_fp32_tflops"] / (fp32_peak.value / 1e12)
     # ---- e2e through the public C-ABI with pinned host buffers

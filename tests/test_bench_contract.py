@@ -29,6 +29,11 @@ def test_work_per_iteration(bench):
     assert [bench.flops_per_solve_iter_3d(n) for n in (8, 16, 24)] == [17491, 196139, 735363]
     # no polynomial: the plain inner CG iteration costs what the FP64 one does
     assert bench.inner_flops_per_iter(32, 0) == bench.flops_per_solve_iter(32)
+    # two-level V-cycle, smoothing degree 2 (M = 3), coarse spacing 4 at N = 32:
+    # 7 stencils, 52 vector operations per node, 7 x 7 coarse nodes
+    assert bench.inner_flops_per_iter(32, 2, 4) == 7 * 2 * 91 ** 2 + 52 * 31 ** 2 + 2 * 49 ** 2 + 28 * 49
+    # a coarse grid without interior nodes leaves the smoother's count
+    assert bench.inner_flops_per_iter(6, 2, 4) == bench.inner_flops_per_iter(6, 2)
 
 
 def test_reference_arm_json_line(built, tmp_path):
