@@ -1920,7 +1920,7 @@ int msfem_autotune(msfem_handle *h, const msfem_batch_desc *d, int32_t sample_ce
         if (cands[v].poly > 0) {
           // two-level shapes smooth with a narrower interval than the
           // polynomial preconditioner alone
-          const std::vector<float> ratios = cands[v].coarse > 0 ? std::vector<float>{10.0f, 15.0f, 25.0f}
+          const std::vector<float> ratios = cands[v].coarse > 0 ? std::vector<float>{12.0f, 15.0f, 20.0f}
                                                                  : std::vector<float>{10.0f, 30.0f, 100.0f};
           for (float ratio : ratios) {
             Tune t;

@@ -1673,56 +1673,51 @@ msfem2d_mixed_kernel(const KernelParams p) {
         float *__restrict__ Lb = reinterpret_cast<float *>(ub);
         float *__restrict__ invd = Lb + C::NI * (W + 1);
         const float *__restrict__ A1 = a1;
-        if (warp == 0) {
+        // warp 0 factors column k while warp 1 computes row k - 1 of
+        // X = L^-1 (which needs only the factor's rows up to k - 1), stored
+        // transposed (XT[j][k] = X[k][j], row j of a0); a two-warp named
+        // barrier per step orders them (measured faster than one warp
+        // doing both, or X by columns after the factorisation)
+        if (warp < 2) {
+          float *__restrict__ XT = a0;
 #pragma unroll 1
-          for (int k = 0; k < nI; ++k) {
-            const int i = k + lane;
-            float sp = 0.0f;
-            if (lane <= W && i < nI) {
-              sp = 0.5f * (A1[i * nI + k] + A1[k * nI + i]);
-#pragma unroll
-              for (int q = 1; q <= W; ++q)
-                if (q <= W - lane && k - q >= 0) sp = fmaf(-Lb[i * (W + 1) + W - lane - q], Lb[k * (W + 1) + W - q], sp);
-            }
-            const float piv = __shfl_sync(0xffffffffu, sp, 0);
-            const float id = piv > 0.0f ? rsqrtf(piv) : 0.0f;  // a lost pivot drops that coarse mode
-            if (lane == 0) {
-              Lb[k * (W + 1) + W] = piv * id;
-              invd[k] = id;
-            } else if (lane <= W && i < nI) {
-              Lb[i * (W + 1) + W - lane] = sp * id;
-            }
-            __syncwarp();
-          }
-        }
-        __syncthreads();
-        if (tid < nI) {
-          // column j of X = L^-1 by forward substitution in blocks of W
-          // steps (the W-value window of the recurrence stays in
-          // registers), stored as row j of a0 (measured faster than
-          // computing the rows of X inside the factorisation loop)
-          float *__restrict__ row = a0 + tid * nI;
-          float win[W];
-#pragma unroll
-          for (int q = 0; q < W; ++q) win[q] = 0.0f;
-#pragma unroll 1
-          for (int kb = 0; kb < nI; kb += W) {
-#pragma unroll
-            for (int u = 0; u < W; ++u) {
-              const int k = kb + u;
-              float yk = 0.0f;
+          for (int k = 0; k <= nI; ++k) {
+            if (warp == 0) {
               if (k < nI) {
-                float s = k == tid ? 1.0f : 0.0f;
+                const int i = k + lane;
+                float sp = 0.0f;
+                if (lane <= W && i < nI) {
+                  sp = 0.5f * (A1[i * nI + k] + A1[k * nI + i]);
 #pragma unroll
-                for (int q = W; q >= 1; --q)  // newest term last: shorter dependency chain
-                  if (k - q >= 0) s = fmaf(-Lb[k * (W + 1) + W - q], win[(u - q + W) % W], s);
-                yk = s * invd[k];
+                  for (int q = 1; q <= W; ++q)
+                    if (q <= W - lane && k - q >= 0) sp = fmaf(-Lb[i * (W + 1) + W - lane - q], Lb[k * (W + 1) + W - q], sp);
+                }
+                const float piv = __shfl_sync(0xffffffffu, sp, 0);
+                const float id = piv > 0.0f ? rsqrtf(piv) : 0.0f;  // a lost pivot drops that coarse mode
+                if (lane == 0) {
+                  Lb[k * (W + 1) + W] = piv * id;
+                  invd[k] = id;
+                } else if (lane <= W && i < nI) {
+                  Lb[i * (W + 1) + W - lane] = sp * id;
+                }
               }
-              win[u] = yk;
-            }
+            } else {
+              const int kk = k - 1;
+              if (kk >= 0) {
 #pragma unroll
-            for (int u = 0; u < W; ++u)
-              if (kb + u < nI) row[kb + u] = win[u];
+                for (int h = 0; h < 2; ++h) {
+                  const int j = lane + 32 * h;
+                  if (j < nI) {
+                    float sx = kk == j ? 1.0f : 0.0f;
+#pragma unroll
+                    for (int q = W; q >= 1; --q)  // newest term last
+                      if (kk - q >= 0) sx = fmaf(-Lb[kk * (W + 1) + W - q], XT[j * nI + kk - q], sx);
+                    XT[j * nI + kk] = sx * invd[kk];
+                  }
+                }
+              }
+            }
+            asm volatile("bar.sync 1, 64;" ::: "memory");  // warps 0 and 1, same count in both
           }
         }
         __syncthreads();
