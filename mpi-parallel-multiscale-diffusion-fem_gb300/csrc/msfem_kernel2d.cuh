@@ -53,9 +53,10 @@ struct Smem2D {
 // Coarse-grid arrays of the two-level preconditioner (mixed form), after the
 // second FP32 exchange buffer.  Coarse spacing CH fine cells, so at most
 // NC = NMAX / CH coarse intervals and NI = (NC - 1)^2 interior coarse nodes:
-//   ub  [NC][2][32] float4  row-block partial restrictions (lower / upper
-//                           coarse row, by fine column); during the set-up the
-//                           band Cholesky factor of Ac
+//   ub  [2][NC][33] float4  row-block partial restrictions onto the lower /
+//                           upper coarse row, by fine column (rows of 33: the
+//                           per-coarse-node column sums read distinct banks);
+//                           during the set-up the band Cholesky factor of Ac
 //   rc  [NI] float4         restricted residual, 4 RHS
 //   ec  [NC+1][NC+1] float4 coarse correction with a zero boundary ring
 //   a0  [NI][NI] float      set-up scratch: row j = column j of L^-1 (Ac = L L^T)
@@ -66,7 +67,7 @@ struct Coarse2D {
   static constexpr int NC = CH > 0 ? NMAX / CH : 2;
   static constexpr int NI = (NC - 1) * (NC - 1);
   static constexpr size_t kUB = L::kEndCheb;
-  static constexpr size_t kRC = L::al(kUB + 16 * 2 * 32 * NC);
+  static constexpr size_t kRC = L::al(kUB + 16 * 2 * 33 * NC);
   static constexpr size_t kEC = L::al(kRC + 16 * NI);
   static constexpr size_t kA0 = L::al(kEC + 16 * (NC + 1) * (NC + 1));
   static constexpr size_t kA1 = L::al(kA0 + sizeof(float) * NI * NI);
@@ -1545,8 +1546,8 @@ msfem2d_mixed_kernel(const KernelParams p) {
             hi[r] = fmaf(wh, e[s][r], hi[r]);
           }
         }
-        ub[(2 * blk) * 32 + col] = make_float4(lo[0], lo[1], lo[2], lo[3]);
-        ub[(2 * blk + 1) * 32 + col] = make_float4(hi[0], hi[1], hi[2], hi[3]);
+        ub[blk * 33 + col] = make_float4(lo[0], lo[1], lo[2], lo[3]);
+        ub[(C::NC + blk) * 33 + col] = make_float4(hi[0], hi[1], hi[2], hi[3]);
       }
       __syncthreads();
       if (tid < nI) {
@@ -1556,7 +1557,7 @@ msfem2d_mixed_kernel(const KernelParams p) {
         for (int d = 1 - CH; d <= CH - 1; ++d) {
           const float w = (float)(CH - (d < 0 ? -d : d)) * (1.0f / (CH > 0 ? CH : 1));
           const int c = CH * cx + d - 1;  // lane of fine column CH cx + d
-          const float4 u0 = ub[(2 * cy) * 32 + c], u1 = ub[(2 * cy - 1) * 32 + c];
+          const float4 u0 = ub[cy * 33 + c], u1 = ub[(C::NC + cy - 1) * 33 + c];
           a.x = fmaf(w, u0.x + u1.x, a.x);
           a.y = fmaf(w, u0.y + u1.y, a.y);
           a.z = fmaf(w, u0.z + u1.z, a.z);
@@ -1573,6 +1574,7 @@ msfem2d_mixed_kernel(const KernelParams p) {
         const int i = tid >> 2, q = tid & 3;
         float a[4] = {0.f, 0.f, 0.f, 0.f};
         if (i < nI)
+#pragma unroll 4
           for (int j = q; j < nI; j += 4) {
             const float w = Aci[i * nI + j];
             const float4 v = rcs[j];
