@@ -302,6 +302,13 @@ int msfem_autotune(msfem_handle *handle, const msfem_batch_desc *desc,
 /* Install a launch choice (e.g. one saved from an earlier msfem_autotune). */
 int msfem_set_tuning(msfem_handle *handle, const msfem_tuning *tuning);
 
+/* Describe a compiled launch shape without running anything: for the key
+ * (dim, n_max, precision) and variant of *tuning, fill the output fields
+ * threads, rows_per_thread, ctas_per_sm, n_variants, poly_degree,
+ * cluster_ctas and coarse_spacing; the other fields are left as given.
+ * MSFEM_ERR_INVALID_ARG for an unknown key or a variant out of range. */
+int msfem_describe_tuning(msfem_tuning *tuning);
+
 /* Number of doubles msfem_tabulate_coefficient writes for this batch. */
 int64_t msfem_tabulated_size(const msfem_batch_desc *desc, int32_t ncomp);
 

@@ -138,6 +138,7 @@ class Tuning(ctypes.Structure):
 
 # Every entry point include/msfem_gpu.h declares: name -> (restype, argtypes)
 EXPORTS = {
+    "msfem_describe_tuning": (ctypes.c_int, [ctypes.POINTER(Tuning)]),
     "msfem_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int]),
     "msfem_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "msfem_set_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),

@@ -1879,6 +1879,24 @@ int msfem_set_tuning(msfem_handle *h, const msfem_tuning *t) {
   return MSFEM_OK;
 }
 
+int msfem_describe_tuning(msfem_tuning *t) {
+  if (!t) return fail(MSFEM_ERR_INVALID_ARG, "tuning is required");
+  if (t->dim != 2 && t->dim != 3) return fail(MSFEM_ERR_INVALID_ARG, "tuning dim must be 2 or 3");
+  const bool mixed = t->precision == MSFEM_PREC_MIXED;
+  const std::vector<Launch> c = candidates(t->dim, t->n_max, mixed);
+  if (t->variant < 0 || t->variant >= (int)c.size())
+    return fail(MSFEM_ERR_INVALID_ARG, "tuning variant out of range");
+  const Launch &L = c[t->variant];
+  t->n_variants = (int)c.size();
+  t->threads = L.nt;
+  t->rows_per_thread = L.rows;
+  t->ctas_per_sm = L.minb;
+  t->poly_degree = L.poly;
+  t->cluster_ctas = L.cluster;
+  t->coarse_spacing = L.coarse;
+  return MSFEM_OK;
+}
+
 int msfem_autotune(msfem_handle *h, const msfem_batch_desc *d, int32_t sample_cells,
                    msfem_tuning *result) {
   if (!h) return fail(MSFEM_ERR_INVALID_ARG, "handle is NULL");

@@ -208,6 +208,18 @@ class Engine:
         if rc != _abi.OK:
             raise _abi.MsfemError(rc, _abi.last_error(self.lib))
 
+    def describe_tuning(self, tuning):
+        """The compiled launch shape behind a tuning key and variant: its
+        threads, strip height, occupancy, polynomial degree, cluster size and
+        coarse spacing, and the number of shapes for the key."""
+        t = _abi.Tuning()
+        for k, v in tuning.items():
+            setattr(t, k, v)
+        rc = self.lib.msfem_describe_tuning(ctypes.byref(t))
+        if rc != _abi.OK:
+            raise _abi.MsfemError(rc, _abi.last_error(self.lib))
+        return t.as_dict()
+
     def tabulate(self, problem, ncomp):
         keep = []
         d = self.make_desc(problem, keep=keep)

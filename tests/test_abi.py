@@ -89,6 +89,37 @@ def test_invalid_descriptors_are_rejected_without_a_gpu(built):
     assert lib.msfem_last_error(buf, 256) == 0
 
 
+def test_describe_tuning_lists_the_compiled_shapes(built):
+    """msfem_describe_tuning reports a compiled shape without a GPU: the
+    N <= 32 mixed class holds the polynomial shapes and the two-level one
+    (degree-2 smoothing, coarse spacing 4); bad keys are argument errors."""
+    abi = built._abi
+    lib = abi.load()
+
+    def describe(**kw):
+        t = abi.Tuning()
+        for k, v in kw.items():
+            setattr(t, k, v)
+        rc = lib.msfem_describe_tuning(ctypes.byref(t))
+        return rc, t.as_dict()
+
+    rc, first = describe(dim=2, n_max=32, precision=abi.PREC_MIXED, variant=0)
+    assert rc == 0 and first["n_variants"] >= 2
+    shapes = [describe(dim=2, n_max=32, precision=abi.PREC_MIXED, variant=v)[1] for v in range(first["n_variants"])]
+    two_level = [t for t in shapes if t["coarse_spacing"] > 0]
+    assert [(t["coarse_spacing"], t["poly_degree"], t["threads"], t["rows_per_thread"]) for t in two_level] == [(4, 2, 256, 4)]
+    assert any(t["poly_degree"] == 5 and t["coarse_spacing"] == 0 for t in shapes)
+    rc, fp64 = describe(dim=2, n_max=32, precision=abi.PREC_FP64, variant=0)
+    assert rc == 0 and fp64["coarse_spacing"] == 0 and fp64["poly_degree"] == 0
+    rc, c3 = describe(dim=3, n_max=24, precision=abi.PREC_MIXED, variant=0)
+    assert rc == 0 and c3["n_variants"] >= 1
+    assert max(describe(dim=3, n_max=24, precision=abi.PREC_MIXED, variant=v)[1]["cluster_ctas"]
+               for v in range(c3["n_variants"])) == 8
+    assert describe(dim=2, n_max=32, precision=abi.PREC_MIXED, variant=first["n_variants"])[0] == abi.ERR_INVALID_ARG
+    assert describe(dim=4, n_max=32, precision=abi.PREC_MIXED, variant=0)[0] == abi.ERR_INVALID_ARG
+    assert lib.msfem_describe_tuning(None) == abi.ERR_INVALID_ARG
+
+
 def test_create_without_device_fails_cleanly(built):
     """On a machine without a GB300 msfem_create must fail with NO_DEVICE (or
     succeed on an sm_103 box) -- never fall back to the CPU."""

@@ -66,6 +66,34 @@ def test_random_fourier_tensor_parity(pkg, oracle, engine, precision):
     check(got, ref)
 
 
+def test_two_level_shape_cuts_inner_iterations(pkg, oracle, engine):
+    """The two-level inner preconditioner (Chebyshev smoothing around the
+    Galerkin coarse correction) meets the oracle like every shape, with well
+    under half the inner iterations of the degree-5 Chebyshev shape on
+    random-Fourier cells (a broken coarse correction would still converge,
+    only slowly)."""
+    W = pkg.workloads
+    prob = W.subset(W.fourier_square(K=64, N=32), [0, 1, 63, 64, 700, 2080, 3333, 4095])
+    ref = oracle.run(prob)
+    key = {"dim": 2, "n_max": 32, "precision": 1}
+    n = engine.describe_tuning(dict(key, variant=0))["n_variants"]
+    shapes = [dict(engine.describe_tuning(dict(key, variant=v)), variant=v) for v in range(n)]
+    two = [t for t in shapes if t["coarse_spacing"] > 0]
+    cheb = [t for t in shapes if t["poly_degree"] == 5 and t["coarse_spacing"] == 0 and t["ctas_per_sm"] == 1
+            and t["threads"] == 256]
+    assert two and cheb
+    iters = {}
+    try:
+        for name, shape, ratio in (("two-level", two[0], 20.0), ("chebyshev", cheb[0], 100.0)):
+            engine.set_tuning(dict(key, variant=shape["variant"], check_interval=0, inner_tol=1e-5, cheb_ratio=ratio))
+            got = engine.run(prob, precision="mixed", tol=1e-10)
+            check(got, ref, basis=False)
+            iters[name] = int(got["stats"]["iterations_total"])
+    finally:
+        engine.set_tuning(dict(key, variant=0, check_interval=0, inner_tol=1e-6))
+    assert iters["two-level"] < 0.5 * iters["chebyshev"], iters
+
+
 def test_tabulation_matches_oracle(pkg, oracle, engine):
     """The field generator against the oracle's direct evaluation: affine
     cells take the phase-recurrence path, a bilinear cell the per-point one."""
