@@ -1503,7 +1503,8 @@ msfem2d_mixed_kernel(const KernelParams p) {
     // CH fine cells; coarse row j at fine row CH j is the boundary between
     // strip row-blocks j - 1 and j, so each strip sees exactly coarse rows
     // blk and blk + 1, with bilinear weights (CH - 1 - s) / CH and (s + 1) / CH
-    const int ncg = (CH > 0 && N % (CH > 0 ? CH : 1) == 0) ? N / (CH > 0 ? CH : 1) : 0;
+    constexpr int kCH = CH > 0 ? CH : 1;  // CH as a divisor (the CH = 0 shapes compile this code unused)
+    const int ncg = (CH > 0 && N % kCH == 0) ? N / kCH : 0;
     const bool coarse = CH > 0 && ncg >= 2;
     const int nI = coarse ? (ncg - 1) * (ncg - 1) : 0;
     float4 *ub = reinterpret_cast<float4 *>(smem_raw + C::kUB);
@@ -1515,8 +1516,8 @@ msfem2d_mixed_kernel(const KernelParams p) {
 #pragma unroll
     for (int s = 0; s < S; ++s) sq[s] = sown[s] > 0.0f ? 1.0f / sown[s] : 0.0f;
     // bilinear x weights of the strip's column: coarse columns cxl, cxl + 1
-    const int cxl = CH > 0 ? ix / (CH > 0 ? CH : 1) : 0;
-    const float wxh = CH > 0 ? (float)(ix - CH * cxl) * (1.0f / (CH > 0 ? CH : 1)) : 0.0f, wxl = 1.0f - wxh;
+    const int cxl = CH > 0 ? ix / kCH : 0;
+    const float wxh = CH > 0 ? (float)(ix - CH * cxl) * (1.0f / kCH) : 0.0f, wxl = 1.0f - wxh;
     // one stencil pass y = A~ x through the exchange buffers v32 / v32b in
     // turn: one barrier per pass, since a buffer is written again only after
     // the barrier that follows every read of it
@@ -1538,8 +1539,8 @@ msfem2d_mixed_kernel(const KernelParams p) {
         float lo[4] = {0.f, 0.f, 0.f, 0.f}, hi[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
         for (int s = 0; s < S; ++s) {
-          const float wl = (float)(CH - 1 - s) * (1.0f / (CH > 0 ? CH : 1)) * sq[s];
-          const float wh = (float)(s + 1) * (1.0f / (CH > 0 ? CH : 1)) * sq[s];
+          const float wl = (float)(CH - 1 - s) * (1.0f / kCH) * sq[s];
+          const float wh = (float)(s + 1) * (1.0f / kCH) * sq[s];
 #pragma unroll
           for (int r = 0; r < 4; ++r) {
             lo[r] = fmaf(wl, e[s][r], lo[r]);
@@ -1555,7 +1556,7 @@ msfem2d_mixed_kernel(const KernelParams p) {
         float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
         for (int d = 1 - CH; d <= CH - 1; ++d) {
-          const float w = (float)(CH - (d < 0 ? -d : d)) * (1.0f / (CH > 0 ? CH : 1));
+          const float w = (float)(CH - (d < 0 ? -d : d)) * (1.0f / kCH);
           const int c = CH * cx + d - 1;  // lane of fine column CH cx + d
           const float4 u0 = ub[cy * 33 + c], u1 = ub[(C::NC + cy - 1) * 33 + c];
           a.x = fmaf(w, u0.x + u1.x, a.x);
@@ -1603,7 +1604,7 @@ msfem2d_mixed_kernel(const KernelParams p) {
       }
 #pragma unroll
       for (int s = 0; s < S; ++s) {
-        const float wh = (float)(s + 1) * (1.0f / (CH > 0 ? CH : 1)), wl = 1.0f - wh;
+        const float wh = (float)(s + 1) * (1.0f / kCH), wl = 1.0f - wh;
 #pragma unroll
         for (int r = 0; r < 4; ++r) cr[s][r] = sq[s] * fmaf(wl, bo[r], wh * to[r]);
       }
@@ -1637,7 +1638,7 @@ msfem2d_mixed_kernel(const KernelParams p) {
                 const float wx = a ? wxh : wxl;
 #pragma unroll
                 for (int s = 0; s < S; ++s) {
-                  const float wy = (float)(b ? s + 1 : CH - 1 - s) * (1.0f / CH);
+                  const float wy = (float)(b ? s + 1 : CH - 1 - s) * (1.0f / kCH);
 #pragma unroll
                   for (int r = 0; r < 4; ++r)
                     if (colour == r) v[s][r] = fmaf(sq[s] * wx, wy, v[s][r]);
