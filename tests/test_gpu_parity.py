@@ -94,6 +94,32 @@ def test_two_level_shape_cuts_inner_iterations(pkg, oracle, engine):
     assert iters["two-level"] < 0.5 * iters["chebyshev"], iters
 
 
+def test_two_level_shape_absolute_tolerance(pkg, oracle, engine):
+    """The two-level shape under the reference's absolute stopping rule
+    (SolverControl(1000, 1e-12) on the residual, diffusion_problem_basis.tpp:297)
+    with A = 0.01 I, so ||b|| is well below 1: no more inner iterations than
+    the relative stop, M at the direct solve's value (quadratic in the basis
+    error), F within what the absolute stop allows (linear in the basis
+    error; the stop leaves a relative residual near 1e-12 / ||b||)."""
+    W = pkg.workloads
+    prob = W.problem(2, W.unit_cube_corners(2, 2), 32, {"kind": 0, "params": [0.01, 0.0, 0.01]})
+    key = {"dim": 2, "n_max": 32, "precision": 1}
+    n = engine.describe_tuning(dict(key, variant=0))["n_variants"]
+    v = next(i for i in range(n) if engine.describe_tuning(dict(key, variant=i))["coarse_spacing"] > 0)
+    try:
+        engine.set_tuning(dict(key, variant=v, check_interval=0, inner_tol=1e-5, cheb_ratio=20.0))
+        rel = engine.run(prob, precision="mixed", tol=1e-12)
+        ab = engine.run(prob, precision="mixed", tol=1e-12, tol_absolute=True)
+    finally:
+        engine.set_tuning(dict(key, variant=0, check_interval=0, inner_tol=1e-6))
+    assert rel["rc"] == 0 and ab["rc"] == 0 and np.all(ab["status"] == 0)
+    assert ab["iters"].sum() <= rel["iters"].sum()
+    direct = oracle.run(prob)
+    assert rel_err(ab["M"], direct["M"]) < TOL_REL
+    assert rel_err(ab["F"], direct["F"]) < 1e-8
+    assert rel_err(rel["F"], direct["F"]) < TOL_REL
+
+
 def test_tabulation_matches_oracle(pkg, oracle, engine):
     """The field generator against the oracle's direct evaluation: affine
     cells take the phase-recurrence path, a bilinear cell the per-point one."""
